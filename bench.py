@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark of the RTM hot path: one step = one single-shot migration (forward
+propagation with source-wavefield storage + adjoint propagation with imaging) of the
+3400 x 700 faulted-model workload (dx 5 m, CPML 50, nt 7500, 3400 receivers).
+
+Metric: Gcell-updates/s, where one migration credits 2 * dimX * dimZ * nt cell-updates
+(forward + backward over the padded grid; the source-field reconstruction is not
+credited).  `value` times the device-resident plan API (inputs already in HBM); `e2e`
+times the reference-shaped host entry point rtm_migrate_shot (host buffers, copies in the
+timed region).  `--impl reference` times the CPU implementation of the same path on the
+host cores instead.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+Under torchrun (N > 1) every rank runs independent migrations (replicas, no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+TRAFFIC_SUMMARY = os.path.join(ROOT, "profiles", "k_step_bwd_traffic.txt")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=("gpu", "reference"))
+    ap.add_argument("--workload", default="large", choices=("large", "small"))
+    ap.add_argument("--storage", default="ring", choices=("ring", "snapshot"))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of the bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(args, with_seis=True):
+    """Params and seeded host inputs of the benchmarked workload."""
+    from rtmuq2d_gb300 import workloads
+    import rtmuq2d_gb300 as eng
+    storage = 1 if args.storage == "ring" else 0
+    if args.workload == "large":
+        p = workloads.params_large(storage=storage)
+        true, mig = workloads.models_large(p, seed=1)
+    else:
+        p = workloads.params_small(storage=storage)
+        true, mig = workloads.models_small(p, seed=0)
+    wav = workloads.wavelet_for(p)
+    ext_true = eng.extend_matrix(p, true)
+    ext = eng.extend_matrix(p, mig)
+    return p, ext_true, ext, wav
+
+
+def workload_name(p):
+    return "rtm_single_shot_%dx%d_nt%d" % (p.nx, p.nz, p.nt)
+
+
+def algorithmic_bytes(p):
+    """Algorithmic DRAM bytes per launch of each kernel (FP32 fields, ring storage).
+    k_step forward : 16 B per cell (u_cur, u_prev, coef read; u_next write)
+                     + 12 B per CPML-correction cell (psi read, xi read+write)
+                     + 4 B per ring cell written
+    k_step backward: receiver field as forward (16 B/cell + 12 B/CPML cell)
+                     + 12 B per reconstruction-region cell (S_cur, S_prev read; S_next write)
+                     + 4 B per ring cell read + 4 B per receiver (seismogram row)
+                     + imaging every time_slices steps: 32 B per interior cell (FP64
+                       image and self image read+write), averaged per launch
+    k_psi          : 12 B per psi cell (u read, psi read+write)."""
+    dx, dz = p.dim_x, p.dim_z
+    cells = dx * dz
+    thl, thr, thu, thd = p.th_left, p.th_right, p.th_up, p.th_down
+    corr = (thl - 8) * (dz - 8) + (thr - 8) * (dz - 8) + (thu - 8) * dx + (thd - 8) * (dx - 8)
+    psi = (thl - 8) * (dz - 8) + (thr - 8) * (dz - 8) + (thu - 8) * (dx - 8) + (thd - 8) * (dx - 8)
+    ring = 8 * (p.nx + 16) + 8 * (p.nz + 8)
+    region = (p.nx + 8) * (p.nz + 8)
+    interior = p.nx * p.nz
+    fwd = 16 * cells + 12 * corr + 4 * ring
+    bwd = 16 * cells + 12 * corr + 12 * region + 4 * ring + 4 * p.rec_count + 32 * interior / p.time_slices
+    return {"k_step_fwd": fwd, "k_step_bwd": bwd, "k_psi": 12 * psi}
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per k_step backward launch from the committed ncu summary, if any."""
+    try:
+        with open(TRAFFIC_SUMMARY) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_full_size:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(p, ext, wav, seis, target_s, dtype=np.float32):
+    """Times the CPU implementation (oracle port, OpenMP over all host cores) on a bounded
+    sample of the workload: the same grid, a shortened time axis."""
+    from oracle.oracle import Oracle
+    orc = Oracle(fast=True)
+    threads = orc.max_threads()
+    q = p.as_dict()
+
+    def run(nt):
+        qq = dict(q, nt=nt)
+        s = np.ascontiguousarray(seis[:, :nt]) if seis is not None else np.zeros((p.rec_count, nt), np.float32)
+        t0 = time.perf_counter()
+        fwd = orc.forward(qq, ext, wav, snapshots=True)
+        orc.adjoint(qq, ext, s, fwd["snapshots"])
+        return time.perf_counter() - t0
+
+    nt0 = 40
+    t = run(nt0)
+    per_step = t / nt0
+    nt = int(max(nt0, min(p.nt, target_s / max(per_step, 1e-9))) // p.time_slices * p.time_slices)
+    nt = max(nt, p.time_slices)
+    t = run(nt)
+    cells = 2 * p.dim_x * p.dim_z * nt
+    return {"value": cells / t / 1e9, "unit": "Gcell-updates/s", "cores": threads,
+            "kind": "port", "seconds": t,
+            "sample": "forward+adjoint of the %dx%d padded grid for nt=%d of %d steps "
+                      "(oracle/rtm_oracle.c, -O3 OpenMP)" % (p.dim_x, p.dim_z, nt, p.nt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    p, ext_true, ext, wav = workload(args)
+    rng = np.random.default_rng(5)
+    seis = (rng.standard_normal((p.rec_count, p.nt)) * 1e-3).astype(np.float32)
+    target = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sample(p, ext, wav, seis, target / 4)
+    vals = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_sample(p, ext, wav, seis, target)
+        vals.append(last["value"])
+    v = float(np.mean(vals))
+    cells_per_step = 2 * p.dim_x * p.dim_z * p.nt
+    line = {"impl": "reference", "metric": "RTM Gcell-updates/s (single-shot migration)", "value": v,
+            "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": cells_per_step / (v * 1e9) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
+                       "note": "each step times a bounded sample (shortened time axis) of the workload"},
+            "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": last["cores"],
+                             "kind": last["kind"], "sample": last["sample"]},
+            "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import rtmuq2d_gb300 as eng
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    p, ext_true, ext, wav = workload(args)
+    # observed data: forward modelling on the true model with trace recording (untimed)
+    seis = eng.model_seismogram(p.replace(storage=0), ext_true, wav)
+
+    stream = torch.cuda.Stream()
+    plan = eng.Plan(p)
+    plan.set_stream(stream.cuda_stream)
+    d_vel = torch.from_numpy(ext).cuda()
+    d_wav = torch.from_numpy(wav).cuda()
+    d_seis = torch.from_numpy(seis).cuda()
+    d_img = torch.empty((p.nx, p.nz), dtype=torch.float32, device="cuda")
+    d_slf = torch.empty_like(d_img)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2
+
+    def migrate():
+        plan.forward(d_vel, d_wav)
+        plan.adjoint(d_seis, d_img, d_slf)
+
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        migrate()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    launches0 = plan.launches
+    plan.profile(16)
+    times = []
+    barrier()
+    with sampler:
+        for _ in range(args.steps):
+            flush.fill_(1.0)                      # L2 flush between timed iterations
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            with torch.cuda.stream(stream):
+                migrate()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    barrier()
+    prof = plan.profile_read()
+    plan.profile(0)
+    launches = plan.launches - launches0
+    total_ms = float(sum(times))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    cells = p.cell_updates
+    value = ws * args.steps * cells / (total_ms * 1e-3) / 1e9
+
+    # e2e: the reference-shaped host entry point with host buffers (copies in the timed region)
+    e2e_ms = []
+    img_h = np.zeros((p.nx, p.nz), np.float32)
+    for i in range(1 + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        img_h, slf_h = eng.migrate_shot(p, ext, wav, seis)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i > 0:
+            e2e_ms.append(dt)
+    e2e_total = float(sum(e2e_ms))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = ws * args.steps * cells / (e2e_total * 1e-3) / 1e9
+    # sanity: the device-resident and host paths produce the same image
+    dev_img = d_img.cpu().numpy()
+    agree = float(np.linalg.norm(dev_img - img_h) / max(np.linalg.norm(img_h), 1e-30))
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return 0
+
+    nbytes = algorithmic_bytes(p)
+    bwd_avg_ms = prof["bwd_ms"] / max(prof["bwd_n"], 1)
+    fwd_avg_ms = prof["fwd_ms"] / max(prof["fwd_n"], 1)
+    achieved = nbytes["k_step_bwd"] / (bwd_avg_ms * 1e-3) / 1e9
+    peak, peak_kind = hbm_peak()
+    roofline = {"bound": "hbm", "kernel": "k_step<float,backward>", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_per_launch(), "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": nbytes["k_step_bwd"],
+                "avg_launch_ms": bwd_avg_ms, "sampled_launches": prof["bwd_n"],
+                "fwd_kernel_avg_launch_ms": fwd_avg_ms,
+                "fwd_kernel_achieved_gbs": nbytes["k_step_fwd"] / (fwd_avg_ms * 1e-3) / 1e9,
+                "note": "working set of one 3500x800 grid (~45 MB/step) is L2-resident"}
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
+        cpu.pop("seconds", None)
+    line = {"metric": "RTM Gcell-updates/s (single-shot migration)", "value": value,
+            "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
+                       "receivers": p.rec_count, "storage": args.storage, "ring_precision": "fp32",
+                       "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "flushed between timed iterations (256 MB write)"},
+            "e2e": {"value": e2e_value, "unit": "Gcell-updates/s", "ms_per_step": e2e_total / args.steps,
+                    "h2d_bytes_per_step": int(ext.nbytes + wav.nbytes + seis.nbytes),
+                    "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
+                    "entry_point": "rtm_migrate_shot", "image_agreement_rel_l2": agree},
+            "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": sampler.summary()}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,194 @@
+/*
+ * rtm_gpu.h -- C ABI of the GB300 (sm_103a) engine for 2-D isotropic acoustic
+ * reverse-time migration.  Drop-in for the migration path of rtmUq2D.
+ *
+ * Plain C types only: sizes as ints, host arrays as float*, device arrays as void*
+ * (CUDA device pointers), streams as void* (cudaStream_t).  Every entry point returns an
+ * rtm_status code; none calls exit().
+ *
+ * Layout convention shared with the reference: 2-D arrays are x-major with z
+ * contiguous, element (x, z) at x*dimZ + z, where dimX = th_left + nx + th_right and
+ * dimZ = th_up + nz + th_down (SRC/stencilDFM.c:23).  Images are nx x nz, (x, z) at
+ * x*nz + z (SRC/image_conditions.c:28).  Seismograms are rec_count x nt, (irec, t) at
+ * irec*nt + t (SRC/backward_modeling.c:280).
+ */
+#ifndef RTM_GPU_H
+#define RTM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+typedef enum rtm_status {
+    RTM_OK = 0,
+    RTM_ERR_INVALID = 1,      /* bad argument or unsupported configuration            */
+    RTM_ERR_CUDA = 2,         /* a CUDA runtime/driver call failed                    */
+    RTM_ERR_NOMEM = 3,        /* device allocation failed or admission refused        */
+    RTM_ERR_STATE = 4,        /* call out of order (e.g. adjoint before forward)      */
+    RTM_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (kernel flag)     */
+    RTM_ERR_IO = 6,           /* file missing, short read or write                    */
+    RTM_ERR_DECODE = 7,       /* ZFP stream could not be decoded                      */
+    RTM_ERR_BUSY = 8          /* serving queue full / result not ready                */
+} rtm_status;
+
+/* ---- configuration ------------------------------------------------------------------ */
+enum rtm_storage {            /* how the backward pass gets the source wavefield      */
+    RTM_STORE_SNAPSHOT = 0,   /* interior snapshot every time_slices steps (the        */
+                              /* reference's TEMPORARY_FILES contents, kept in HBM)    */
+    RTM_STORE_RING = 1        /* 4-cell boundary ring every step + reverse-time        */
+                              /* reconstruction of the source field                    */
+};
+enum rtm_precision {          /* element type of stored rings / snapshots             */
+    RTM_PREC_FP32 = 0,
+    RTM_PREC_BF16 = 1,        /* with a per-step, per-tile max-abs scale               */
+    RTM_PREC_FP16 = 2
+};
+enum rtm_compute {            /* wavefield arithmetic                                  */
+    RTM_COMPUTE_FP32 = 0,     /* the reference's precision                             */
+    RTM_COMPUTE_FP64 = 1      /* same scheme in double: the error yardstick            */
+};
+
+/*
+ * Run-time form of SRC/fixed_parameters.h (plus TIME_SLICES from forward_modeling.h:4).
+ * The first 17 fields mirror the reference's constants one for one:
+ *   nx, nz            Nx, Nz
+ *   th_*              thicknessLeft/Right/Up/Down
+ *   dx, dt            spacingGrid, sampling
+ *   nt                numberOfTimeStep
+ *   n_wavelet         sampligWavelet
+ *   shot_x, shot_z    shot[0], shot[1] as passed to isotropicAcousticModeling
+ *   rec_*             firstLocationReceiver, spacingReceiver, numberOfReceivers,
+ *                     depthReceiver
+ *   time_slices       TIME_SLICES (imaging / snapshot interval)
+ */
+typedef struct rtm_params {
+    int nx, nz;
+    int th_left, th_right, th_up, th_down;
+    float dx, dt;
+    int nt, n_wavelet;
+    int shot_x, shot_z;
+    int rec_first, rec_spacing, rec_count, rec_depth;
+    int time_slices;
+    int storage;               /* enum rtm_storage                                    */
+    int precision;             /* enum rtm_precision (stored source wavefield)        */
+    int compute;               /* enum rtm_compute                                    */
+    int tile_x;                /* x columns per CTA tile: 0 = autotuned default        */
+    int reserved[3];
+} rtm_params;
+
+/* Fills *p with the engine's defaults for the fields after time_slices. */
+void rtm_params_defaults(rtm_params *p);
+/* RTM_OK if the engine supports *p (checks sizes, CPML >= 12 cells, positions inside
+ * the grid, nt multiple of time_slices, shot inside the reconstruction region for
+ * RTM_STORE_RING). */
+int rtm_params_check(const rtm_params *p);
+/* Device bytes one migration of *p holds (admission by HBM footprint). */
+long long rtm_footprint_bytes(const rtm_params *p);
+
+const char *rtm_status_string(int status);
+const char *rtm_last_error(void);     /* detail of the last failure on this thread */
+int rtm_device_info(char *name, int name_len, int *sm_count, long long *hbm_bytes);
+
+/* ---- reference-shaped entry points (host buffers) ------------------------------------ */
+
+/* Replaces isotropicAcousticModeling(int simId, int *shot, float *velocity,
+ * float *wavelet) -- SRC/forward_modeling.h:11, forward_modeling.c:12-159.
+ * velocity: padded dimX x dimZ model (what rtm_iso2d.c:85 passes).  The source
+ * wavefield (rings or snapshots) stays in device memory keyed by sim_id, instead of
+ * ./TEMPORARY_FILES/sourceWavefield_<simId>.bin, until rtm_adjoint_modeling consumes it. */
+int rtm_forward_modeling(const rtm_params *p, int sim_id, const int *shot,
+                         const float *velocity, const float *wavelet);
+
+/* Replaces int adjointModeling(int simId, int *shot, float *velocity, float *wavelet,
+ * float *seismogram, float *imageCondition, float *selfImageCondition) --
+ * SRC/backward_modeling.h:11, backward_modeling.c:12-165.  Accumulates into image and
+ * self_image (nx x nz).  Frees the sim_id state.  Returns RTM_OK (the reference
+ * returns 1 whatever happens; rtm_dropin.c keeps that). */
+int rtm_adjoint_modeling(const rtm_params *p, int sim_id, const int *shot,
+                         const float *velocity, const float *wavelet,
+                         const float *seismogram, float *image, float *self_image);
+
+/* Forward + adjoint of one shot in one call (rtm_iso2d.c:85-93 without the decode). */
+int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wavelet,
+                     const float *seismogram, float *image, float *self_image);
+
+/* Forward modelling with trace recording: seismogram[irec*nt + t] = u at the receiver
+ * cells after step t's source injection.  (Not in the reference, whose
+ * forward_modeling.c:92 computes z_receiver but never records; used to make the
+ * observed data that the adjoint pass consumes.) */
+int rtm_model_seismogram(const rtm_params *p, const float *velocity, const float *wavelet,
+                         float *seismogram);
+
+/* One leapfrog step on host buffers -- replaces iso_acoustic_wave_equation(float *pond,
+ * float *waveField2, float *waveField3), SRC/stencilDFM.h:15.  wave3 is overwritten. */
+int rtm_iso_acoustic_wave_equation(const rtm_params *p, const float *pond, const float *wave2,
+                                   float *wave3);
+
+/* One CPML update on host buffers -- replaces aiso_attenuation_cpml(...),
+ * SRC/absorbingBoundaryCondition.h:29, argument order kept; psi/xi strips in the
+ * reference's layouts and updated in place. */
+int rtm_aiso_attenuation_cpml(const rtm_params *p, const float *wave1, float *wave2,
+                              const float *coef,
+                              const float *a_left, const float *b_left,
+                              const float *a_right, const float *b_right,
+                              const float *a_top, const float *b_top,
+                              const float *a_bottom, const float *b_bottom,
+                              float *psi_left, float *psi_right, float *psi_top,
+                              float *psi_bottom, float *xi_left, float *xi_right,
+                              float *xi_top, float *xi_bottom);
+
+/* Host-side set-up, same arithmetic as the reference:
+ *   attenuation_profile_cpml  SRC/absorbingBoundaryCondition.h:27
+ *   extend_matrix             SRC/generic_functions.h:5
+ * laplacian_filter2D (SRC/math_functions.h:15) runs on the GPU. */
+void rtm_attenuation_profile_cpml(const rtm_params *p, float *a_left, float *a_right,
+                                  float *a_top, float *a_bottom, float *b_left,
+                                  float *b_right, float *b_top, float *b_bottom);
+void rtm_extend_matrix(const rtm_params *p, float *extended, const float *model);
+int rtm_laplacian_filter2D(const rtm_params *p, float *lp, const float *image);
+
+/* normalized_cross_correlation(img, self, S, R) -- SRC/image_conditions.h:6: host
+ * buffers, padded S and R, nx x nz images accumulated. */
+int rtm_normalized_cross_correlation(const rtm_params *p, float *image, float *self_image,
+                                     const float *source, const float *receiver);
+
+/* ---- device-resident plan (inputs already in HBM) ------------------------------------ */
+typedef struct rtm_plan rtm_plan;
+
+int rtm_plan_create(const rtm_params *p, rtm_plan **plan);
+int rtm_plan_destroy(rtm_plan *plan);
+int rtm_plan_set_stream(rtm_plan *plan, void *stream);
+/* velocity/wavelet/seismogram/image pointers below are DEVICE pointers (float32,
+ * reference layouts).  image/self_image receive (not accumulate) the nx x nz result. */
+int rtm_plan_forward(rtm_plan *plan, const void *d_velocity, const void *d_wavelet,
+                     void *d_seismogram_out);
+int rtm_plan_adjoint(rtm_plan *plan, const void *d_seismogram, void *d_image,
+                     void *d_self_image);
+/* Device-side wavefield access for tests: which = 0 source field (u_nt after the
+ * forward pass), 1 = its predecessor, 2 = receiver field.  Copies dimX x dimZ values of
+ * the plan's compute type to a device buffer. */
+int rtm_plan_read_field(rtm_plan *plan, int which, void *d_out);
+/* image (which = 0) or self image (which = 1), nx x nz, float or double, to a device
+ * buffer; valid after rtm_plan_adjoint. */
+int rtm_plan_read_image(rtm_plan *plan, int which, int as_double, void *d_out);
+/* Waits for the plan's stream and reports a device-side failure flag. */
+int rtm_plan_sync(rtm_plan *plan);
+/* Number of kernels the plan launched since creation (launch accounting). */
+long long rtm_plan_launch_count(const rtm_plan *plan);
+/* Device bytes the plan holds. */
+long long rtm_plan_bytes(const rtm_plan *plan);
+/* Sampled kernel timing: with every > 0, each step whose index is a multiple of `every`
+ * brackets its fused step kernel with CUDA events on the plan's stream (0 = off).
+ * _read returns the summed milliseconds and launch counts (forward, backward) since the
+ * last call and resets them. */
+int rtm_plan_profile(rtm_plan *plan, int every);
+int rtm_plan_profile_read(rtm_plan *plan, double *fwd_ms, int *fwd_n, double *bwd_ms, int *bwd_n);
+
+/* Frees the plans the host-buffer entry points keep for reuse. */
+void rtm_release_cached(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

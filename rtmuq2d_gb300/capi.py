@@ -1,0 +1,337 @@
+"""ctypes binding of librtmgpu (include/rtm_gpu.h).
+
+Host-array entry points take numpy arrays in the reference's layouts; the plan API takes
+device pointers (ints, or anything with ``data_ptr()`` such as torch tensors).  Every
+call raises ``RtmError`` on a non-zero status.  There is no CPU fallback: if the library
+cannot be loaded, importing the engine fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+RTM_OK = 0
+RTM_ERR_INVALID = 1
+RTM_ERR_CUDA = 2
+RTM_ERR_NOMEM = 3
+RTM_ERR_STATE = 4
+RTM_ERR_TIMEOUT = 5
+RTM_ERR_IO = 6
+RTM_ERR_DECODE = 7
+RTM_ERR_BUSY = 8
+
+STORE_SNAPSHOT = 0
+STORE_RING = 1
+PREC_FP32 = 0
+PREC_BF16 = 1
+PREC_FP16 = 2
+COMPUTE_FP32 = 0
+COMPUTE_FP64 = 1
+
+
+class RtmParams(C.Structure):
+    """Run-time form of the reference's SRC/fixed_parameters.h (see include/rtm_gpu.h)."""
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("th_left", C.c_int), ("th_right", C.c_int),
+                ("th_up", C.c_int), ("th_down", C.c_int), ("dx", C.c_float), ("dt", C.c_float),
+                ("nt", C.c_int), ("n_wavelet", C.c_int), ("shot_x", C.c_int), ("shot_z", C.c_int),
+                ("rec_first", C.c_int), ("rec_spacing", C.c_int), ("rec_count", C.c_int),
+                ("rec_depth", C.c_int), ("time_slices", C.c_int), ("storage", C.c_int),
+                ("precision", C.c_int), ("compute", C.c_int), ("tile_x", C.c_int),
+                ("reserved", C.c_int * 3)]
+
+    @classmethod
+    def make(cls, **kw) -> "RtmParams":
+        p = cls()
+        p.storage, p.precision, p.compute, p.tile_x = STORE_RING, PREC_FP32, COMPUTE_FP32, 0
+        p.time_slices = 20
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+    def replace(self, **kw) -> "RtmParams":
+        q = RtmParams()
+        C.memmove(C.byref(q), C.byref(self), C.sizeof(RtmParams))
+        for k, v in kw.items():
+            setattr(q, k, v)
+        return q
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+    @property
+    def dim_x(self) -> int:
+        return self.th_left + self.nx + self.th_right
+
+    @property
+    def dim_z(self) -> int:
+        return self.th_up + self.nz + self.th_down
+
+    @property
+    def cell_updates(self) -> int:
+        """Credited work of one migration: 2 * dimX * dimZ * nt (forward + backward)."""
+        return 2 * self.dim_x * self.dim_z * self.nt
+
+    def __repr__(self):
+        return "RtmParams(%s)" % ", ".join("%s=%r" % kv for kv in self.as_dict().items())
+
+
+class RtmError(RuntimeError):
+    def __init__(self, status: int, detail: str):
+        super().__init__("%s: %s" % (status_string(status), detail))
+        self.status = status
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """The loaded engine library (built in-tree on first use if absent)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.LIB
+            if not os.path.exists(path):
+                _build.build()
+            L = C.CDLL(path)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def _declare(L):
+    P = C.POINTER(RtmParams)
+    vp, fp, ip = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int)
+    sig = {
+        "rtm_params_defaults": (None, [P]),
+        "rtm_params_check": (C.c_int, [P]),
+        "rtm_footprint_bytes": (C.c_longlong, [P]),
+        "rtm_status_string": (C.c_char_p, [C.c_int]),
+        "rtm_last_error": (C.c_char_p, []),
+        "rtm_device_info": (C.c_int, [C.c_char_p, C.c_int, ip, C.POINTER(C.c_longlong)]),
+        "rtm_forward_modeling": (C.c_int, [P, C.c_int, ip, fp, fp]),
+        "rtm_adjoint_modeling": (C.c_int, [P, C.c_int, ip, fp, fp, fp, fp, fp]),
+        "rtm_migrate_shot": (C.c_int, [P, fp, fp, fp, fp, fp]),
+        "rtm_model_seismogram": (C.c_int, [P, fp, fp, fp]),
+        "rtm_iso_acoustic_wave_equation": (C.c_int, [P, fp, fp, fp]),
+        "rtm_aiso_attenuation_cpml": (C.c_int, [P, fp, fp, fp] + [fp] * 8 + [fp] * 8),
+        "rtm_attenuation_profile_cpml": (None, [P] + [fp] * 8),
+        "rtm_extend_matrix": (None, [P, fp, fp]),
+        "rtm_laplacian_filter2D": (C.c_int, [P, fp, fp]),
+        "rtm_normalized_cross_correlation": (C.c_int, [P, fp, fp, fp, fp]),
+        "rtm_plan_create": (C.c_int, [P, C.POINTER(vp)]),
+        "rtm_plan_destroy": (C.c_int, [vp]),
+        "rtm_plan_set_stream": (C.c_int, [vp, vp]),
+        "rtm_plan_forward": (C.c_int, [vp, vp, vp, vp]),
+        "rtm_plan_adjoint": (C.c_int, [vp, vp, vp, vp]),
+        "rtm_plan_read_field": (C.c_int, [vp, C.c_int, vp]),
+        "rtm_plan_read_image": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+        "rtm_plan_sync": (C.c_int, [vp]),
+        "rtm_plan_launch_count": (C.c_longlong, [vp]),
+        "rtm_plan_bytes": (C.c_longlong, [vp]),
+        "rtm_release_cached": (None, []),
+        "rtm_plan_profile": (C.c_int, [vp, C.c_int]),
+        "rtm_plan_profile_read": (C.c_int, [vp, C.POINTER(C.c_double), ip, C.POINTER(C.c_double), ip]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def exported_symbols():
+    """Names declared in include/rtm_gpu.h that the binding declares."""
+    return ["rtm_params_defaults", "rtm_params_check", "rtm_footprint_bytes", "rtm_status_string",
+            "rtm_last_error", "rtm_device_info", "rtm_forward_modeling", "rtm_adjoint_modeling",
+            "rtm_migrate_shot", "rtm_model_seismogram", "rtm_iso_acoustic_wave_equation",
+            "rtm_aiso_attenuation_cpml", "rtm_attenuation_profile_cpml", "rtm_extend_matrix",
+            "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_plan_create",
+            "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
+            "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_launch_count",
+            "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read"]
+
+
+def status_string(st: int) -> str:
+    return lib().rtm_status_string(st).decode()
+
+
+def _check(st: int) -> None:
+    if st != RTM_OK:
+        raise RtmError(st, lib().rtm_last_error().decode())
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _dev(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    return C.c_void_p(x.data_ptr())
+
+
+# ---- configuration helpers -------------------------------------------------------------------
+def params_check(p: RtmParams) -> None:
+    _check(lib().rtm_params_check(C.byref(p)))
+
+
+def footprint_bytes(p: RtmParams) -> int:
+    return int(lib().rtm_footprint_bytes(C.byref(p)))
+
+
+def device_info():
+    name = C.create_string_buffer(256)
+    sms = C.c_int()
+    mem = C.c_longlong()
+    _check(lib().rtm_device_info(name, 256, C.byref(sms), C.byref(mem)))
+    return {"name": name.value.decode(), "sm_count": sms.value, "hbm_bytes": mem.value}
+
+
+# ---- host-side set-up (same arithmetic as the reference) ------------------------------------
+def attenuation_profile_cpml(p: RtmParams) -> dict:
+    a = {k: np.zeros(n, np.float32) for k, n in
+         (("a_l", p.th_left), ("a_r", p.th_right), ("a_t", p.th_up), ("a_b", p.th_down),
+          ("b_l", p.th_left), ("b_r", p.th_right), ("b_t", p.th_up), ("b_b", p.th_down))}
+    lib().rtm_attenuation_profile_cpml(C.byref(p), *[_fp(a[k]) for k in
+                                       ("a_l", "a_r", "a_t", "a_b", "b_l", "b_r", "b_t", "b_b")])
+    return a
+
+
+def extend_matrix(p: RtmParams, model: np.ndarray) -> np.ndarray:
+    out = np.zeros((p.dim_x, p.dim_z), np.float32)
+    lib().rtm_extend_matrix(C.byref(p), _fp(out), _fp(_f32(model)))
+    return out
+
+
+# ---- reference-shaped entry points on host arrays ------------------------------------------
+def forward_modeling(p: RtmParams, sim_id: int, shot, velocity, wavelet) -> None:
+    """isotropicAcousticModeling: source wavefield stays on the device under sim_id."""
+    s = (C.c_int * 2)(*shot) if shot is not None else None
+    _check(lib().rtm_forward_modeling(C.byref(p), sim_id, s, _fp(_f32(velocity)), _fp(_f32(wavelet))))
+
+
+def adjoint_modeling(p: RtmParams, sim_id: int, shot, velocity, wavelet, seismogram,
+                     image: np.ndarray, self_image: np.ndarray) -> None:
+    """adjointModeling: accumulates into image/self_image (float32, nx x nz, in place)."""
+    s = (C.c_int * 2)(*shot) if shot is not None else None
+    assert image.dtype == np.float32 and image.flags.c_contiguous
+    assert self_image.dtype == np.float32 and self_image.flags.c_contiguous
+    _check(lib().rtm_adjoint_modeling(C.byref(p), sim_id, s, _fp(_f32(velocity)), _fp(_f32(wavelet)),
+                                      _fp(_f32(seismogram)), _fp(image), _fp(self_image)))
+
+
+def migrate_shot(p: RtmParams, velocity, wavelet, seismogram):
+    img = np.zeros((p.nx, p.nz), np.float32)
+    slf = np.zeros((p.nx, p.nz), np.float32)
+    _check(lib().rtm_migrate_shot(C.byref(p), _fp(_f32(velocity)), _fp(_f32(wavelet)),
+                                  _fp(_f32(seismogram)), _fp(img), _fp(slf)))
+    return img, slf
+
+
+def model_seismogram(p: RtmParams, velocity, wavelet) -> np.ndarray:
+    seis = np.zeros((p.rec_count, p.nt), np.float32)
+    _check(lib().rtm_model_seismogram(C.byref(p), _fp(_f32(velocity)), _fp(_f32(wavelet)), _fp(seis)))
+    return seis
+
+
+def iso_acoustic_wave_equation(p: RtmParams, pond, wave2, wave3) -> np.ndarray:
+    out = np.array(wave3, np.float32, copy=True)
+    _check(lib().rtm_iso_acoustic_wave_equation(C.byref(p), _fp(_f32(pond)), _fp(_f32(wave2)), _fp(out)))
+    return out
+
+
+def aiso_attenuation_cpml(p: RtmParams, wave1, wave2, coef, prof: dict, psi: dict, xi: dict):
+    out = np.array(wave2, np.float32, copy=True)
+    _check(lib().rtm_aiso_attenuation_cpml(
+        C.byref(p), _fp(_f32(wave1)), _fp(out), _fp(_f32(coef)),
+        _fp(prof["a_l"]), _fp(prof["b_l"]), _fp(prof["a_r"]), _fp(prof["b_r"]),
+        _fp(prof["a_t"]), _fp(prof["b_t"]), _fp(prof["a_b"]), _fp(prof["b_b"]),
+        _fp(psi["l"]), _fp(psi["r"]), _fp(psi["t"]), _fp(psi["b"]),
+        _fp(xi["l"]), _fp(xi["r"]), _fp(xi["t"]), _fp(xi["b"])))
+    return out
+
+
+def normalized_cross_correlation(p: RtmParams, image, self_image, source, receiver) -> None:
+    _check(lib().rtm_normalized_cross_correlation(C.byref(p), _fp(image), _fp(self_image),
+                                                  _fp(_f32(source)), _fp(_f32(receiver))))
+
+
+def laplacian_filter2D(p: RtmParams, image) -> np.ndarray:
+    out = np.zeros((p.nx, p.nz), np.float32)
+    _check(lib().rtm_laplacian_filter2D(C.byref(p), _fp(out), _fp(_f32(image))))
+    return out
+
+
+def release_cached() -> None:
+    lib().rtm_release_cached()
+
+
+# ---- device-resident plan -----------------------------------------------------------------
+class Plan:
+    """One migration's device state (include/rtm_gpu.h, rtm_plan_*)."""
+
+    def __init__(self, p: RtmParams):
+        self.params = p.replace()
+        h = C.c_void_p()
+        _check(lib().rtm_plan_create(C.byref(self.params), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().rtm_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int):
+        _check(lib().rtm_plan_set_stream(self.handle, C.c_void_p(stream_ptr)))
+
+    def forward(self, d_velocity, d_wavelet, d_seismogram_out=None):
+        _check(lib().rtm_plan_forward(self.handle, _dev(d_velocity), _dev(d_wavelet),
+                                      _dev(d_seismogram_out)))
+
+    def adjoint(self, d_seismogram, d_image=None, d_self_image=None):
+        _check(lib().rtm_plan_adjoint(self.handle, _dev(d_seismogram), _dev(d_image), _dev(d_self_image)))
+
+    def read_field(self, which: int, d_out):
+        _check(lib().rtm_plan_read_field(self.handle, which, _dev(d_out)))
+
+    def read_image(self, which: int, d_out, as_double: bool = False):
+        _check(lib().rtm_plan_read_image(self.handle, which, int(as_double), _dev(d_out)))
+
+    def sync(self):
+        _check(lib().rtm_plan_sync(self.handle))
+
+    def profile(self, every: int):
+        _check(lib().rtm_plan_profile(self.handle, every))
+
+    def profile_read(self):
+        fm, bm = C.c_double(), C.c_double()
+        fn, bn = C.c_int(), C.c_int()
+        _check(lib().rtm_plan_profile_read(self.handle, C.byref(fm), C.byref(fn), C.byref(bm), C.byref(bn)))
+        return {"fwd_ms": fm.value, "fwd_n": fn.value, "bwd_ms": bm.value, "bwd_n": bn.value}
+
+    @property
+    def launches(self) -> int:
+        return int(lib().rtm_plan_launch_count(self.handle))
+
+    @property
+    def nbytes(self) -> int:
+        return int(lib().rtm_plan_bytes(self.handle))

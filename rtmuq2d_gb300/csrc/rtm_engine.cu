@@ -1,0 +1,1119 @@
+// rtm_engine.cu -- host side of the RTM engine: plans (device state of one migration),
+// the forward / adjoint time loops, and the C ABI declared in include/rtm_gpu.h.
+//
+// The time loops replace SRC/forward_modeling.c:98-130 and SRC/backward_modeling.c:268-297.
+// One step = k_psi (CPML psi update) + k_step (everything else, fused).  The forward
+// pass leaves u_nt, u_{nt-1} and the stored source wavefield (rings or snapshots) in HBM;
+// the adjoint pass consumes them in place of ./TEMPORARY_FILES.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rtm_gpu.h"
+#include "rtm_internal.h"
+
+namespace rtm {
+
+// ---- errors ------------------------------------------------------------------------------
+static thread_local std::string t_err;
+
+static int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+#define RTM_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(e_ == cudaErrorMemoryAllocation ? RTM_ERR_NOMEM : RTM_ERR_CUDA,        \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+    } while (0)
+
+#define RTM_TRY(expr)                                                                           \
+    do {                                                                                        \
+        int s_ = (expr);                                                                        \
+        if (s_ != RTM_OK) return s_;                                                            \
+    } while (0)
+
+// ---- tensor maps (driver entry point, no libcuda link) ----------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tensor_map_encoder()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// 2-D map over a pitched field: dims {pitch (z), dimx (x)}, box {SZ, tx+8}, zero fill.
+static int make_field_map(CUtensorMap *m, void *base, const Geom &g, size_t es)
+{
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return fail(RTM_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)g.pitch, (cuuint64_t)g.dimx};
+    cuuint64_t strides[1] = {(cuuint64_t)g.pitch * es};
+    cuuint32_t box[2] = {(cuuint32_t)SZ, (cuuint32_t)(g.tx + 2 * HALO)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                     2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(RTM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return RTM_OK;
+}
+
+// ---- geometry and validation ----------------------------------------------------------------
+static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+static int default_tile_x(const rtm_params &p)
+{
+    (void)p;
+    return 32;
+}
+
+static Geom make_geom(const rtm_params &p)
+{
+    Geom g;
+    memset(&g, 0, sizeof g);
+    g.nx = p.nx; g.nz = p.nz;
+    g.thl = p.th_left; g.thr = p.th_right; g.thu = p.th_up; g.thd = p.th_down;
+    g.dimx = g.thl + g.nx + g.thr;
+    g.dimz = g.thu + g.nz + g.thd;
+    g.pitch = round_up(g.dimz, 32);
+    g.st = round_up(g.thu, 4);
+    g.sb = round_up(g.thd, 4);
+    g.xs = p.shot_x + g.thl;
+    g.zs = p.shot_z + g.thu;
+    g.zrec = g.thu + p.rec_depth;
+    g.rx0 = g.thl - 4; g.rx1 = g.dimx - g.thr + 4;
+    g.rz0 = g.thu - 4; g.rz1 = g.dimz - g.thd + 4;
+    g.ring_w = g.rx1 - g.rx0 + 8;
+    g.ring_h = g.rz1 - g.rz0;
+    g.ring_cells = 8 * g.ring_w + 8 * g.ring_h;
+    g.nt = p.nt; g.nwav = p.n_wavelet; g.slices = p.time_slices; g.nrec = p.rec_count;
+    g.tx = p.tile_x > 0 ? p.tile_x : default_tile_x(p);
+    g.tiles_x = (g.dimx + g.tx - 1) / g.tx;
+    g.tiles_z = (g.dimz + TZ - 1) / TZ;
+    return g;
+}
+
+static int check_params(const rtm_params &p)
+{
+    if (p.nx < 1 || p.nz < 1) return fail(RTM_ERR_INVALID, "nx, nz must be >= 1");
+    if (p.th_left < 12 || p.th_right < 12 || p.th_up < 12 || p.th_down < 12)
+        return fail(RTM_ERR_INVALID, "every CPML thickness must be >= 12 cells");
+    if (!(p.dx > 0.0f) || !(p.dt > 0.0f)) return fail(RTM_ERR_INVALID, "dx and dt must be > 0");
+    if (p.nt < 1) return fail(RTM_ERR_INVALID, "nt must be >= 1");
+    if (p.n_wavelet < 0) return fail(RTM_ERR_INVALID, "n_wavelet must be >= 0");
+    if (p.time_slices < 1) return fail(RTM_ERR_INVALID, "time_slices must be >= 1");
+    if (p.nt % p.time_slices != 0)
+        return fail(RTM_ERR_INVALID, "nt (%d) must be a multiple of time_slices (%d)", p.nt,
+                    p.time_slices);
+    if (p.rec_count < 0) return fail(RTM_ERR_INVALID, "rec_count must be >= 0");
+    if (p.storage != RTM_STORE_SNAPSHOT && p.storage != RTM_STORE_RING)
+        return fail(RTM_ERR_INVALID, "unknown storage %d", p.storage);
+    if (p.precision < RTM_PREC_FP32 || p.precision > RTM_PREC_FP16)
+        return fail(RTM_ERR_INVALID, "unknown precision %d", p.precision);
+    if (p.compute != RTM_COMPUTE_FP32 && p.compute != RTM_COMPUTE_FP64)
+        return fail(RTM_ERR_INVALID, "unknown compute type %d", p.compute);
+    if (p.compute == RTM_COMPUTE_FP64 && p.precision != RTM_PREC_FP32)
+        return fail(RTM_ERR_INVALID, "16-bit storage needs FP32 compute");
+    if (p.tile_x != 0 && p.tile_x != 8 && p.tile_x != 16 && p.tile_x != 32)
+        return fail(RTM_ERR_INVALID, "tile_x must be 0, 8, 16 or 32");
+    const long long dimx = (long long)p.th_left + p.nx + p.th_right;
+    const long long dimz = (long long)p.th_up + p.nz + p.th_down;
+    if (dimx * (long long)round_up((int)dimz, 32) > (1ll << 31) - 1)
+        return fail(RTM_ERR_INVALID, "grid too large");
+    const Geom g = make_geom(p);
+    if (g.xs < 0 || g.xs >= g.dimx || g.zs < 0 || g.zs >= g.dimz)
+        return fail(RTM_ERR_INVALID, "shot cell (%d,%d) outside the padded grid", g.xs, g.zs);
+    if (p.storage == RTM_STORE_RING &&
+        !(g.xs >= g.rx0 && g.xs < g.rx1 && g.zs >= g.rz0 && g.zs < g.rz1))
+        return fail(RTM_ERR_INVALID, "ring storage needs the shot inside the stencil-only region");
+    if (p.rec_count > 0) {
+        if (g.zrec < 0 || g.zrec >= g.dimz) return fail(RTM_ERR_INVALID, "receiver depth outside the grid");
+        const long long c0 = (long long)p.th_left + p.rec_first;
+        const long long c1 = c0 + (long long)(p.rec_spacing - 1) * (p.rec_count - 1);
+        if (std::min(c0, c1) < 0 || std::max(c0, c1) >= g.dimx)
+            return fail(RTM_ERR_INVALID, "receiver line outside the grid");
+        if ((long long)p.rec_count * p.nt > (1ll << 31) - 1)
+            return fail(RTM_ERR_INVALID, "seismogram too large");
+    }
+    return RTM_OK;
+}
+
+// ---- device memory layout of one plan ----------------------------------------------------
+struct Layout {
+    size_t u[2], r[2], coef, strips, strip_bytes, prof, rec, wav, seis_t, img, slf, store,
+        store_bytes, scales, staging, status, total;
+    size_t psi[4], xi[4];
+    int nslots;
+    size_t slot_elems;   // elements per storage slot
+    size_t n_scales_per_slot;
+};
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static Layout make_layout(const rtm_params &p, const Geom &g)
+{
+    Layout L;
+    memset(&L, 0, sizeof L);
+    const size_t es = p.compute == RTM_COMPUTE_FP64 ? 8 : 4;
+    const size_t se = p.precision == RTM_PREC_FP32 ? es : 2;
+    const size_t field = (size_t)g.dimx * g.pitch * es;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
+    L.u[0] = take(field); L.u[1] = take(field);
+    L.r[0] = take(field); L.r[1] = take(field);
+    L.coef = take(field);
+    const size_t n_l = (size_t)g.thl * g.pitch, n_r = (size_t)g.thr * g.pitch;
+    const size_t n_t = (size_t)g.dimx * g.st, n_b = (size_t)g.dimx * g.sb;
+    L.strips = off;
+    L.psi[0] = take(n_l * es); L.psi[1] = take(n_r * es); L.psi[2] = take(n_t * es); L.psi[3] = take(n_b * es);
+    L.xi[0] = take(n_l * es); L.xi[1] = take(n_r * es); L.xi[2] = take(n_t * es); L.xi[3] = take(n_b * es);
+    L.strip_bytes = off - L.strips;
+    L.prof = take(sizeof(float) * 2 * (size_t)(g.thl + g.thr + g.thu + g.thd));
+    L.rec = take(sizeof(int) * 3 * (size_t)g.dimx);
+    L.wav = take(sizeof(float) * (size_t)std::max(p.n_wavelet, 1));
+    L.seis_t = take(sizeof(float) * (size_t)std::max(1, p.rec_count) * p.nt);
+    L.img = take(sizeof(double) * (size_t)g.nx * g.pitch);
+    L.slf = take(sizeof(double) * (size_t)g.nx * g.pitch);
+    if (p.storage == RTM_STORE_RING) {
+        L.nslots = p.nt + 1;
+        L.slot_elems = (size_t)g.ring_cells;
+    } else {
+        L.nslots = (p.nt + p.time_slices - 1) / p.time_slices;
+        L.slot_elems = (size_t)g.nx * g.pitch;
+    }
+    L.store_bytes = (size_t)L.nslots * L.slot_elems * se;
+    L.store = take(L.store_bytes);
+    L.n_scales_per_slot = (size_t)g.tiles_x * g.tiles_z;
+    L.scales = take(p.precision == RTM_PREC_FP32 ? 0 : sizeof(float) * L.nslots * L.n_scales_per_slot);
+    const size_t stage = std::max({(size_t)g.dimx * g.dimz, (size_t)std::max(1, p.rec_count) * p.nt,
+                                   (size_t)2 * g.nx * g.nz});
+    L.staging = take(stage * sizeof(float) * (es / 4));
+    L.status = take(256);
+    L.total = off;
+    return L;
+}
+
+// ---- plan ---------------------------------------------------------------------------------
+}  // namespace rtm
+
+struct rtm_plan {
+    rtm_params p;
+    rtm::Geom g;
+    rtm::Layout L;
+    size_t es = 4;
+    unsigned char *base = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    CUtensorMap tm_u[2], tm_r[2];
+    int cur_u = 0;        // u buffer holding u_nt after the forward pass
+    int cur_r = 0;        // r buffer holding the last receiver field
+    bool forward_done = false;
+    bool image_valid = false;
+    long long launches = 0;
+    std::vector<float> h_prof;
+    float *h_pinned = nullptr;   // pinned staging for host-buffer entry points
+    size_t h_pinned_bytes = 0;
+    // sampled per-launch timing of k_step (CUDA events on the plan's stream)
+    int prof_every = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_launch[2];   // [forward, backward]
+
+    template <typename T> T *at(size_t off) { return reinterpret_cast<T *>(base + off); }
+
+    cudaEvent_t next_event()
+    {
+        if (ev_used == ev_pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            ev_pool.push_back(e);
+        }
+        return ev_pool[ev_used++];
+    }
+};
+
+namespace rtm {
+
+static int plan_alloc(const rtm_params &p, rtm_plan **out)
+{
+    RTM_TRY(check_params(p));
+    std::unique_ptr<rtm_plan> P(new rtm_plan());
+    P->p = p;
+    P->g = make_geom(p);
+    P->L = make_layout(p, P->g);
+    P->es = p.compute == RTM_COMPUTE_FP64 ? 8 : 4;
+    cudaError_t e = cudaMalloc(&P->base, P->L.total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RTM_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", P->L.total, cudaGetErrorString(e));
+    }
+    for (int i = 0; i < 2; ++i) {
+        RTM_TRY(make_field_map(&P->tm_u[i], P->base + P->L.u[i], P->g, P->es));
+        RTM_TRY(make_field_map(&P->tm_r[i], P->base + P->L.r[i], P->g, P->es));
+    }
+    RTM_CUDA(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    P->own_stream = true;
+    // CPML profiles (host, reference arithmetic) and receiver maps
+    const Geom &g = P->g;
+    std::vector<float> prof(2 * (size_t)(g.thl + g.thr + g.thu + g.thd));
+    float *a_l = prof.data(), *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
+    float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
+    rtm_attenuation_profile_cpml(&p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
+    P->h_prof = prof;
+    std::vector<int> rec(3 * (size_t)g.dimx, 0);
+    int *last = rec.data(), *first = last + g.dimx, *cnt = first + g.dimx;
+    for (int x = 0; x < g.dimx; ++x) { last[x] = -1; first[x] = -1; }
+    for (int i = 0; i < p.rec_count; ++i) {
+        const int x = g.thl + p.rec_first + (p.rec_spacing - 1) * i;  // backward_modeling.c:279
+        last[x] = i;
+        if (cnt[x] == 0) first[x] = i;
+        cnt[x]++;
+    }
+    RTM_CUDA(cudaMemcpyAsync(P->base + P->L.prof, prof.data(), prof.size() * sizeof(float),
+                             cudaMemcpyHostToDevice, P->stream));
+    RTM_CUDA(cudaMemcpyAsync(P->base + P->L.rec, rec.data(), rec.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, P->stream));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.status, 0, 256, P->stream));
+    RTM_CUDA(cudaStreamSynchronize(P->stream));
+    *out = P.release();
+    return RTM_OK;
+}
+
+static void plan_free(rtm_plan *P)
+{
+    if (!P) return;
+    if (P->stream) cudaStreamSynchronize(P->stream);
+    if (P->base) cudaFree(P->base);
+    if (P->h_pinned) cudaFreeHost(P->h_pinned);
+    for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
+    if (P->own_stream && P->stream) cudaStreamDestroy(P->stream);
+    delete P;
+}
+
+static int pinned(rtm_plan *P, size_t bytes, float **out)
+{
+    if (P->h_pinned_bytes < bytes) {
+        if (P->h_pinned) cudaFreeHost(P->h_pinned);
+        P->h_pinned = nullptr;
+        P->h_pinned_bytes = 0;
+        RTM_CUDA(cudaMallocHost(&P->h_pinned, bytes));
+        P->h_pinned_bytes = bytes;
+    }
+    *out = P->h_pinned;
+    return RTM_OK;
+}
+
+template <typename T>
+static void fill_common(rtm_plan *P, StepArgs<T> &a)
+{
+    memset(&a, 0, sizeof a);
+    const Geom &g = P->g;
+    a.g = g;
+    const T dx = (T)P->p.dx;
+    a.h1 = (T)1.0f / dx;
+    a.h2 = dx * dx;
+    a.h3 = (T)1.0f / (dx * dx);
+    a.coef = P->at<T>(P->L.coef);
+    a.psi_l = P->at<T>(P->L.psi[0]); a.psi_r = P->at<T>(P->L.psi[1]);
+    a.psi_t = P->at<T>(P->L.psi[2]); a.psi_b = P->at<T>(P->L.psi[3]);
+    a.xi_l = P->at<T>(P->L.xi[0]); a.xi_r = P->at<T>(P->L.xi[1]);
+    a.xi_t = P->at<T>(P->L.xi[2]); a.xi_b = P->at<T>(P->L.xi[3]);
+    const float *prof = P->at<float>(P->L.prof);
+    a.a_l = prof; a.b_l = prof + g.thl; a.a_r = a.b_l + g.thl; a.b_r = a.a_r + g.thr;
+    a.a_t = a.b_r + g.thr; a.b_t = a.a_t + g.thu; a.a_b = a.b_t + g.thu; a.b_b = a.a_b + g.thd;
+    const int *rec = P->at<int>(P->L.rec);
+    a.rec_last = rec; a.rec_first = rec + g.dimx; a.rec_cnt = rec + 2 * g.dimx;
+    a.store_prec = P->p.precision;
+    a.img = P->at<double>(P->L.img);
+    a.slf = P->at<double>(P->L.slf);
+    a.status = P->at<unsigned>(P->L.status);
+}
+
+template <typename T>
+static void fill_psi(rtm_plan *P, const StepArgs<T> &a, PsiArgs<T> &q)
+{
+    memset(&q, 0, sizeof q);
+    q.g = a.g;
+    q.h1 = a.h1;
+    q.psi_l = const_cast<T *>(a.psi_l); q.psi_r = const_cast<T *>(a.psi_r);
+    q.psi_t = const_cast<T *>(a.psi_t); q.psi_b = const_cast<T *>(a.psi_b);
+    q.a_l = a.a_l; q.b_l = a.b_l; q.a_r = a.a_r; q.b_r = a.b_r;
+    q.a_t = a.a_t; q.b_t = a.b_t; q.a_b = a.a_b; q.b_b = a.b_b;
+    (void)P;
+}
+
+static void *slot_ptr(rtm_plan *P, int slot)
+{
+    const size_t se = P->p.precision == RTM_PREC_FP32 ? P->es : 2;
+    return P->base + P->L.store + (size_t)slot * P->L.slot_elems * se;
+}
+
+static float *scale_ptr(rtm_plan *P, int slot)
+{
+    if (P->p.precision == RTM_PREC_FP32) return nullptr;
+    return P->at<float>(P->L.scales) + (size_t)slot * P->L.n_scales_per_slot;
+}
+
+// k_step launch, bracketed by CUDA events on sampled steps when profiling is on.
+template <typename T>
+static int timed_step(rtm_plan *P, int backward, int step, const CUtensorMap *tm_u,
+                      const CUtensorMap *tm_s, const StepArgs<T> &a)
+{
+    const bool sample = P->prof_every > 0 && step % P->prof_every == 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (sample) {
+        e0 = P->next_event();
+        e1 = P->next_event();
+        if (!e0 || !e1) return fail(RTM_ERR_CUDA, "event pool");
+        RTM_CUDA(cudaEventRecord(e0, P->stream));
+    }
+    RTM_CUDA(launch_step<T>(backward, tm_u, tm_s, a, P->stream));
+    if (sample) {
+        RTM_CUDA(cudaEventRecord(e1, P->stream));
+        P->prof_launch[backward ? 1 : 0].push_back({e0, e1});
+    }
+    return RTM_OK;
+}
+
+// Forward pass: SRC/forward_modeling.c:12-159 on the device.
+template <typename T>
+static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const float *d_wav,
+                       T *d_seis_out)
+{
+    const Geom &g = P->g;
+    cudaStream_t s = P->stream;
+    T *u[2] = {P->at<T>(P->L.u[0]), P->at<T>(P->L.u[1])};
+    RTM_CUDA(launch_coef<T>(g, d_vel, vel_pitch, P->at<T>(P->L.coef), P->p.dx, P->p.dt, s));
+    P->launches++;
+    RTM_CUDA(cudaMemsetAsync(u[0], 0, (size_t)g.dimx * g.pitch * sizeof(T), s));
+    RTM_CUDA(cudaMemsetAsync(u[1], 0, (size_t)g.dimx * g.pitch * sizeof(T), s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.strips, 0, P->L.strip_bytes, s));
+    StepArgs<T> a;
+    fill_common<T>(P, a);
+    a.wavelet = d_wav;
+    a.rec_out = d_seis_out;
+    PsiArgs<T> q;
+    fill_psi<T>(P, a, q);
+    const bool ring = P->p.storage == RTM_STORE_RING;
+    int c = 0;
+    for (int t = 0; t < g.nt; ++t) {
+        q.u = u[c];
+        RTM_CUDA(launch_psi<T>(q, s));
+        a.u_next = u[1 - c];
+        a.t = t;
+        int f = 0;
+        if (t < g.nwav) f |= F_SRC;
+        if (d_seis_out && g.nrec > 0) f |= F_RECORD;
+        a.store = nullptr;
+        a.store_scale = nullptr;
+        if (ring) {
+            f |= F_RING_SAVE;
+            a.store = slot_ptr(P, t + 1);
+            a.store_scale = scale_ptr(P, t + 1);
+        } else if (t % g.slices == 0) {
+            f |= F_SNAP_SAVE;
+            a.store = slot_ptr(P, t / g.slices);
+            a.store_scale = scale_ptr(P, t / g.slices);
+        }
+        a.flags = f;
+        RTM_TRY(timed_step<T>(P, 0, t, &P->tm_u[c], &P->tm_u[c], a));
+        P->launches += 2;
+        c ^= 1;
+    }
+    P->cur_u = c;
+    P->forward_done = true;
+    P->image_valid = false;
+    return RTM_OK;
+}
+
+static int check_status(rtm_plan *P)
+{
+    unsigned st = 0;
+    RTM_CUDA(cudaMemcpyAsync(&st, P->base + P->L.status, sizeof st, cudaMemcpyDeviceToHost, P->stream));
+    RTM_CUDA(cudaStreamSynchronize(P->stream));
+    if (st & ST_TMA_TIMEOUT) {
+        cudaMemsetAsync(P->base + P->L.status, 0, sizeof st, P->stream);
+        return fail(RTM_ERR_TIMEOUT, "a tile load did not complete within its time limit");
+    }
+    return RTM_OK;
+}
+
+// Adjoint pass: SRC/backward_modeling.c:12-165 on the device.  d_seis: [irec][nt].
+template <typename T>
+static int run_adjoint(rtm_plan *P, const float *d_seis)
+{
+    if (!P->forward_done) return fail(RTM_ERR_STATE, "adjoint pass without a forward pass");
+    const Geom &g = P->g;
+    cudaStream_t s = P->stream;
+    T *u[2] = {P->at<T>(P->L.u[0]), P->at<T>(P->L.u[1])};
+    T *r[2] = {P->at<T>(P->L.r[0]), P->at<T>(P->L.r[1])};
+    float *seis_t = P->at<float>(P->L.seis_t);
+    if (g.nrec > 0) {
+        RTM_CUDA(launch_transpose(d_seis, seis_t, g.nrec, g.nt, s));
+        P->launches++;
+    }
+    RTM_CUDA(cudaMemsetAsync(r[0], 0, (size_t)g.dimx * g.pitch * sizeof(T), s));
+    RTM_CUDA(cudaMemsetAsync(r[1], 0, (size_t)g.dimx * g.pitch * sizeof(T), s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.strips, 0, P->L.strip_bytes, s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.img, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.slf, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
+    StepArgs<T> a;
+    fill_common<T>(P, a);
+    a.wavelet = P->at<float>(P->L.wav);
+    PsiArgs<T> q;
+    fill_psi<T>(P, a, q);
+    const bool ring = P->p.storage == RTM_STORE_RING;
+    const int ua = P->cur_u, ub = 1 - P->cur_u;   // u_nt, u_{nt-1}
+    int sc = ub, sp = ua;                          // reconstruction: current / previous
+    int c = 0;
+    int ctrl = g.nt / g.slices - 1;                // backward_modeling.c:267
+    for (int time = 0; time < g.nt; ++time) {
+        const int tau = g.nt - time - 1;
+        int f = F_OVERWRITE;
+        a.seis_row = seis_t + (size_t)tau * std::max(g.nrec, 1);
+        if (g.nrec == 0) f &= ~F_OVERWRITE;
+        a.t = time;
+        a.store = nullptr;
+        a.store_scale = nullptr;
+        a.s_next = nullptr;
+        a.s_snap = nullptr;
+        a.s_fixed = nullptr;
+        const bool recon = ring && time >= 2;
+        if (recon) {
+            f |= F_RECON;
+            if (tau + 2 < g.nwav) f |= F_RECON_SRC;
+            a.s_next = u[sp];
+            a.store = slot_ptr(P, tau + 1);
+            a.store_scale = scale_ptr(P, tau + 1);
+        }
+        if (tau % g.slices == 0) {
+            if (ctrl >= 0) {
+                f |= F_IMAGE;
+                if (!ring) {
+                    f |= F_IMAGE_SNAP;
+                    a.s_snap = reinterpret_cast<const T *>(slot_ptr(P, ctrl));
+                    a.store = slot_ptr(P, ctrl);
+                    a.store_scale = scale_ptr(P, ctrl);
+                } else if (!recon) {
+                    f |= F_IMAGE_FIXED;
+                    a.s_fixed = time == 0 ? u[ua] : u[ub];
+                }
+            }
+            ctrl--;
+        }
+        a.flags = f;
+        q.u = r[c];
+        RTM_CUDA(launch_psi<T>(q, s));
+        a.u_next = r[1 - c];
+        RTM_TRY(timed_step<T>(P, 1, time, &P->tm_r[c], &P->tm_u[sc], a));
+        P->launches += 2;
+        c ^= 1;
+        if (recon) std::swap(sc, sp);
+    }
+    P->cur_r = c;
+    P->forward_done = false;   // the stored source wavefield has been consumed
+    P->image_valid = true;
+    return RTM_OK;
+}
+
+template <typename T>
+static int plan_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const float *d_wav,
+                        void *d_seis_out)
+{
+    // The adjoint pass undoes the source term during reconstruction: keep the wavelet.
+    float *wav = P->at<float>(P->L.wav);
+    if (P->g.nwav > 0 && d_wav != wav)
+        RTM_CUDA(cudaMemcpyAsync(wav, d_wav, sizeof(float) * P->g.nwav, cudaMemcpyDeviceToDevice,
+                                 P->stream));
+    return run_forward<T>(P, d_vel, vel_pitch, wav, reinterpret_cast<T *>(d_seis_out));
+}
+
+static int dispatch_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const float *d_wav,
+                            void *d_seis_out)
+{
+    if (P->es == 8) return plan_forward<double>(P, d_vel, vel_pitch, d_wav, d_seis_out);
+    return plan_forward<float>(P, d_vel, vel_pitch, d_wav, d_seis_out);
+}
+
+static int dispatch_adjoint(rtm_plan *P, const float *d_seis)
+{
+    if (P->es == 8) return run_adjoint<double>(P, d_seis);
+    return run_adjoint<float>(P, d_seis);
+}
+
+// Image (float, nx x nz) from the FP64 accumulators.
+static int image_to(rtm_plan *P, int which, void *d_out, int as_double, int accumulate)
+{
+    if (!P->image_valid) return fail(RTM_ERR_STATE, "no image: run the adjoint pass first");
+    const double *src = P->at<double>(which ? P->L.slf : P->L.img);
+    if (as_double) RTM_CUDA(launch_image_out<double>(P->g, src, (double *)d_out, accumulate, P->stream));
+    else RTM_CUDA(launch_image_out<float>(P->g, src, (float *)d_out, accumulate, P->stream));
+    P->launches++;
+    return RTM_OK;
+}
+
+// ---- plan cache for the host-buffer entry points -------------------------------------
+static std::mutex g_mu;
+static std::map<int, rtm_plan *> g_sim;           // sim_id -> plan holding a forward state
+static std::vector<rtm_plan *> g_idle;            // finished plans kept for reuse
+
+static bool same_params(const rtm_params &a, const rtm_params &b)
+{
+    return memcmp(&a, &b, sizeof a) == 0;
+}
+
+static int acquire_plan(const rtm_params &p, rtm_plan **out)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        for (size_t i = 0; i < g_idle.size(); ++i)
+            if (same_params(g_idle[i]->p, p)) {
+                *out = g_idle[i];
+                g_idle.erase(g_idle.begin() + i);
+                return RTM_OK;
+            }
+    }
+    return plan_alloc(p, out);
+}
+
+static void release_plan(rtm_plan *P)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_idle.push_back(P);
+    while (g_idle.size() > 2) {
+        plan_free(g_idle.front());
+        g_idle.erase(g_idle.begin());
+    }
+}
+
+static int upload_host(rtm_plan *P, void *dst, const void *src, size_t bytes)
+{
+    float *h;
+    RTM_TRY(pinned(P, bytes, &h));
+    RTM_CUDA(cudaStreamSynchronize(P->stream));   // pinned staging is free again
+    memcpy(h, src, bytes);
+    RTM_CUDA(cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, P->stream));
+    return RTM_OK;
+}
+
+static int forward_host(rtm_plan *P, const float *velocity, const float *wavelet, void *d_seis)
+{
+    const Geom &g = P->g;
+    float *stage = P->at<float>(P->L.staging);
+    RTM_TRY(upload_host(P, stage, velocity, sizeof(float) * (size_t)g.dimx * g.dimz));
+    float *wav = P->at<float>(P->L.wav);
+    if (g.nwav > 0) {
+        RTM_CUDA(cudaStreamSynchronize(P->stream));
+        RTM_CUDA(cudaMemcpyAsync(wav, wavelet, sizeof(float) * g.nwav, cudaMemcpyHostToDevice, P->stream));
+    }
+    return dispatch_forward(P, stage, g.dimz, wav, d_seis);
+}
+
+static int adjoint_host(rtm_plan *P, const float *seismogram, float *image, float *self_image)
+{
+    const Geom &g = P->g;
+    float *stage = P->at<float>(P->L.staging);
+    if (g.nrec > 0) RTM_TRY(upload_host(P, stage, seismogram, sizeof(float) * (size_t)g.nrec * g.nt));
+    RTM_TRY(dispatch_adjoint(P, stage));
+    const size_t n = (size_t)g.nx * g.nz;
+    RTM_TRY(image_to(P, 0, stage, 0, 0));
+    RTM_TRY(image_to(P, 1, stage + n, 0, 0));
+    float *h;
+    RTM_TRY(pinned(P, 2 * n * sizeof(float), &h));
+    RTM_CUDA(cudaMemcpyAsync(h, stage, 2 * n * sizeof(float), cudaMemcpyDeviceToHost, P->stream));
+    RTM_TRY(check_status(P));
+    // imageCondition[i] += ..., selfImageCondition[i] += ... (image_conditions.c:28-30)
+    for (size_t i = 0; i < n; ++i) image[i] = image[i] + h[i];
+    for (size_t i = 0; i < n; ++i) self_image[i] = self_image[i] + h[n + i];
+    return RTM_OK;
+}
+
+}  // namespace rtm
+
+using namespace rtm;
+
+// ================================ C ABI ======================================================
+extern "C" {
+
+void rtm_params_defaults(rtm_params *p)
+{
+    p->storage = RTM_STORE_RING;
+    p->precision = RTM_PREC_FP32;
+    p->compute = RTM_COMPUTE_FP32;
+    p->tile_x = 0;
+    p->reserved[0] = p->reserved[1] = p->reserved[2] = 0;
+}
+
+int rtm_params_check(const rtm_params *p)
+{
+    if (!p) return fail(RTM_ERR_INVALID, "null params");
+    return check_params(*p);
+}
+
+long long rtm_footprint_bytes(const rtm_params *p)
+{
+    if (!p || check_params(*p) != RTM_OK) return -1;
+    const Geom g = make_geom(*p);
+    return (long long)make_layout(*p, g).total;
+}
+
+const char *rtm_status_string(int status)
+{
+    switch (status) {
+    case RTM_OK: return "ok";
+    case RTM_ERR_INVALID: return "invalid argument";
+    case RTM_ERR_CUDA: return "CUDA error";
+    case RTM_ERR_NOMEM: return "out of device memory";
+    case RTM_ERR_STATE: return "call out of order";
+    case RTM_ERR_TIMEOUT: return "device wait timed out";
+    case RTM_ERR_IO: return "I/O error";
+    case RTM_ERR_DECODE: return "decode error";
+    case RTM_ERR_BUSY: return "busy";
+    default: return "unknown status";
+    }
+}
+
+const char *rtm_last_error(void) { return t_err.c_str(); }
+
+int rtm_device_info(char *name, int name_len, int *sm_count, long long *hbm_bytes)
+{
+    int dev = 0;
+    RTM_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    RTM_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (name && name_len > 0) snprintf(name, name_len, "%s", prop.name);
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (hbm_bytes) *hbm_bytes = (long long)prop.totalGlobalMem;
+    return RTM_OK;
+}
+
+int rtm_plan_create(const rtm_params *p, rtm_plan **plan)
+{
+    if (!p || !plan) return fail(RTM_ERR_INVALID, "null argument");
+    return plan_alloc(*p, plan);
+}
+
+int rtm_plan_destroy(rtm_plan *plan)
+{
+    plan_free(plan);
+    return RTM_OK;
+}
+
+int rtm_plan_set_stream(rtm_plan *plan, void *stream)
+{
+    if (!plan) return fail(RTM_ERR_INVALID, "null plan");
+    RTM_CUDA(cudaStreamSynchronize(plan->stream));
+    if (plan->own_stream) cudaStreamDestroy(plan->stream);
+    plan->stream = (cudaStream_t)stream;
+    plan->own_stream = false;
+    return RTM_OK;
+}
+
+int rtm_plan_forward(rtm_plan *plan, const void *d_velocity, const void *d_wavelet,
+                     void *d_seismogram_out)
+{
+    if (!plan || !d_velocity || (!d_wavelet && plan->g.nwav > 0))
+        return fail(RTM_ERR_INVALID, "null argument");
+    return dispatch_forward(plan, (const float *)d_velocity, plan->g.dimz, (const float *)d_wavelet,
+                            d_seismogram_out);
+}
+
+int rtm_plan_adjoint(rtm_plan *plan, const void *d_seismogram, void *d_image, void *d_self_image)
+{
+    if (!plan || (!d_seismogram && plan->g.nrec > 0)) return fail(RTM_ERR_INVALID, "null argument");
+    if (!plan->forward_done) return fail(RTM_ERR_STATE, "adjoint pass without a forward pass");
+    // the wavelet of the forward pass is needed for the source term of the reconstruction
+    RTM_TRY(dispatch_adjoint(plan, (const float *)d_seismogram));
+    if (d_image) RTM_TRY(image_to(plan, 0, d_image, 0, 0));
+    if (d_self_image) RTM_TRY(image_to(plan, 1, d_self_image, 0, 0));
+    return check_status(plan);
+}
+
+int rtm_plan_read_image(rtm_plan *plan, int which, int as_double, void *d_out)
+{
+    if (!plan || !d_out) return fail(RTM_ERR_INVALID, "null argument");
+    return image_to(plan, which, d_out, as_double, 0);
+}
+
+int rtm_plan_read_field(rtm_plan *plan, int which, void *d_out)
+{
+    if (!plan || !d_out) return fail(RTM_ERR_INVALID, "null argument");
+    const size_t off = which == 0 ? plan->L.u[plan->cur_u]
+                     : which == 1 ? plan->L.u[1 - plan->cur_u]
+                                  : plan->L.r[1 - plan->cur_r];
+    if (plan->es == 8) RTM_CUDA(launch_field_out<double>(plan->g, plan->at<double>(off), (double *)d_out, plan->stream));
+    else RTM_CUDA(launch_field_out<float>(plan->g, plan->at<float>(off), (float *)d_out, plan->stream));
+    plan->launches++;
+    RTM_CUDA(cudaStreamSynchronize(plan->stream));
+    return RTM_OK;
+}
+
+int rtm_plan_sync(rtm_plan *plan)
+{
+    if (!plan) return fail(RTM_ERR_INVALID, "null plan");
+    return check_status(plan);
+}
+
+long long rtm_plan_launch_count(const rtm_plan *plan) { return plan ? plan->launches : -1; }
+
+int rtm_plan_profile(rtm_plan *plan, int every)
+{
+    if (!plan || every < 0) return fail(RTM_ERR_INVALID, "bad argument");
+    RTM_CUDA(cudaStreamSynchronize(plan->stream));
+    plan->prof_every = every;
+    plan->ev_used = 0;
+    plan->prof_launch[0].clear();
+    plan->prof_launch[1].clear();
+    return RTM_OK;
+}
+
+int rtm_plan_profile_read(rtm_plan *plan, double *fwd_ms, int *fwd_n, double *bwd_ms, int *bwd_n)
+{
+    if (!plan) return fail(RTM_ERR_INVALID, "null plan");
+    RTM_CUDA(cudaStreamSynchronize(plan->stream));
+    double ms[2] = {0.0, 0.0};
+    for (int k = 0; k < 2; ++k)
+        for (auto &pr : plan->prof_launch[k]) {
+            float v = 0.0f;
+            RTM_CUDA(cudaEventElapsedTime(&v, pr.first, pr.second));
+            ms[k] += v;
+        }
+    if (fwd_ms) *fwd_ms = ms[0];
+    if (fwd_n) *fwd_n = (int)plan->prof_launch[0].size();
+    if (bwd_ms) *bwd_ms = ms[1];
+    if (bwd_n) *bwd_n = (int)plan->prof_launch[1].size();
+    plan->ev_used = 0;
+    plan->prof_launch[0].clear();
+    plan->prof_launch[1].clear();
+    return RTM_OK;
+}
+
+long long rtm_plan_bytes(const rtm_plan *plan) { return plan ? (long long)plan->L.total : -1; }
+
+// ---- reference-shaped host-buffer entry points ------------------------------------------
+static rtm_params with_shot(const rtm_params *p, const int *shot)
+{
+    rtm_params q = *p;
+    if (shot) { q.shot_x = shot[0]; q.shot_z = shot[1]; }
+    return q;
+}
+
+int rtm_forward_modeling(const rtm_params *p, int sim_id, const int *shot, const float *velocity,
+                         const float *wavelet)
+{
+    if (!p || !velocity || (!wavelet && p->n_wavelet > 0)) return fail(RTM_ERR_INVALID, "null argument");
+    const rtm_params q = with_shot(p, shot);
+    rtm_plan *P = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_sim.find(sim_id);
+        if (it != g_sim.end()) {          // a forward state nobody consumed: replace it
+            P = it->second;
+            g_sim.erase(it);
+        }
+    }
+    if (P && !same_params(P->p, q)) { plan_free(P); P = nullptr; }
+    if (!P) RTM_TRY(acquire_plan(q, &P));
+    int st = forward_host(P, velocity, wavelet, nullptr);
+    if (st != RTM_OK) { release_plan(P); return st; }
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_sim[sim_id] = P;
+    return RTM_OK;
+}
+
+int rtm_adjoint_modeling(const rtm_params *p, int sim_id, const int *shot, const float *velocity,
+                         const float *wavelet, const float *seismogram, float *image,
+                         float *self_image)
+{
+    (void)velocity; (void)wavelet;   // the forward pass already holds coef and the wavelet
+    if (!p || !image || !self_image || (!seismogram && p->rec_count > 0))
+        return fail(RTM_ERR_INVALID, "null argument");
+    rtm_plan *P = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_sim.find(sim_id);
+        if (it == g_sim.end()) return fail(RTM_ERR_STATE, "no forward state for simulation %d", sim_id);
+        P = it->second;
+        g_sim.erase(it);
+    }
+    if (!same_params(P->p, with_shot(p, shot))) {
+        release_plan(P);
+        return fail(RTM_ERR_INVALID, "parameters differ from the forward pass of simulation %d", sim_id);
+    }
+    const int st = adjoint_host(P, seismogram, image, self_image);
+    release_plan(P);
+    return st;
+}
+
+int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wavelet,
+                     const float *seismogram, float *image, float *self_image)
+{
+    if (!p || !velocity || !image || !self_image) return fail(RTM_ERR_INVALID, "null argument");
+    rtm_plan *P = nullptr;
+    RTM_TRY(acquire_plan(*p, &P));
+    int st = forward_host(P, velocity, wavelet, nullptr);
+    if (st == RTM_OK) st = adjoint_host(P, seismogram, image, self_image);
+    release_plan(P);
+    return st;
+}
+
+int rtm_model_seismogram(const rtm_params *p, const float *velocity, const float *wavelet,
+                         float *seismogram)
+{
+    if (!p || !velocity || !seismogram) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "host recording is FP32");
+    rtm_plan *P = nullptr;
+    RTM_TRY(acquire_plan(*p, &P));
+    const size_t n = (size_t)p->rec_count * p->nt;
+    float *d_seis = nullptr;
+    int st = RTM_OK;
+    if (cudaMalloc(&d_seis, std::max<size_t>(n, 1) * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        release_plan(P);
+        return fail(RTM_ERR_NOMEM, "seismogram buffer");
+    }
+    st = forward_host(P, velocity, wavelet, n ? d_seis : nullptr);
+    if (st == RTM_OK && n) {
+        if (cudaMemcpyAsync(seismogram, d_seis, n * sizeof(float), cudaMemcpyDeviceToHost, P->stream) != cudaSuccess)
+            st = fail(RTM_ERR_CUDA, "seismogram download");
+    }
+    if (st == RTM_OK) st = check_status(P);
+    P->forward_done = false;
+    cudaFree(d_seis);
+    release_plan(P);
+    return st;
+}
+
+void rtm_release_cached(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (rtm_plan *P : g_idle) plan_free(P);
+    g_idle.clear();
+    for (auto &kv : g_sim) plan_free(kv.second);
+    g_sim.clear();
+}
+
+}  // extern "C"
+
+// ---- per-step drop-ins on host buffers (parity and unit testing of single steps) -------
+namespace rtm {
+
+// A plan sized for one step of *p: no receivers, one storage slot.
+static int step_plan(const rtm_params *p, rtm_plan **out)
+{
+    rtm_params q = *p;
+    q.nt = 1; q.time_slices = 1; q.n_wavelet = 0; q.rec_count = 0;
+    q.shot_x = 0; q.shot_z = 0;
+    q.storage = RTM_STORE_SNAPSHOT; q.precision = RTM_PREC_FP32; q.compute = RTM_COMPUTE_FP32;
+    return acquire_plan(q, out);
+}
+
+// host [dimx][dimz] -> pitched device field
+static int field_from_host(rtm_plan *P, float *dst, const float *src)
+{
+    float *stage = P->at<float>(P->L.staging);
+    RTM_TRY(upload_host(P, stage, src, sizeof(float) * (size_t)P->g.dimx * P->g.dimz));
+    RTM_CUDA(launch_field_in<float>(P->g, stage, dst, P->stream));
+    P->launches++;
+    return RTM_OK;
+}
+
+static int field_to_host(rtm_plan *P, float *dst, const float *src)
+{
+    float *stage = P->at<float>(P->L.staging);
+    RTM_CUDA(launch_field_out<float>(P->g, src, stage, P->stream));
+    P->launches++;
+    RTM_CUDA(cudaMemcpyAsync(dst, stage, sizeof(float) * (size_t)P->g.dimx * P->g.dimz,
+                             cudaMemcpyDeviceToHost, P->stream));
+    RTM_CUDA(cudaStreamSynchronize(P->stream));
+    return RTM_OK;
+}
+
+// strip arrays between the reference layouts and the pitched device layouts
+static int strips_io(rtm_plan *P, int to_device, float *const host[8])
+{
+    const Geom &g = P->g;
+    struct { size_t off; int rows, host_w, dev_w; } s[8] = {
+        {P->L.psi[0], g.thl, g.dimz, g.pitch}, {P->L.psi[1], g.thr, g.dimz, g.pitch},
+        {P->L.psi[2], g.dimx, g.thu, g.st},    {P->L.psi[3], g.dimx, g.thd, g.sb},
+        {P->L.xi[0], g.thl, g.dimz, g.pitch},  {P->L.xi[1], g.thr, g.dimz, g.pitch},
+        {P->L.xi[2], g.dimx, g.thu, g.st},     {P->L.xi[3], g.dimx, g.thd, g.sb}};
+    for (int i = 0; i < 8; ++i) {
+        void *dev = P->base + s[i].off;
+        if (to_device) {
+            RTM_CUDA(cudaMemsetAsync(dev, 0, (size_t)s[i].rows * s[i].dev_w * sizeof(float), P->stream));
+            RTM_CUDA(cudaMemcpy2DAsync(dev, s[i].dev_w * sizeof(float), host[i], s[i].host_w * sizeof(float),
+                                       s[i].host_w * sizeof(float), s[i].rows, cudaMemcpyHostToDevice, P->stream));
+        } else {
+            RTM_CUDA(cudaMemcpy2DAsync(host[i], s[i].host_w * sizeof(float), dev, s[i].dev_w * sizeof(float),
+                                       s[i].host_w * sizeof(float), s[i].rows, cudaMemcpyDeviceToHost, P->stream));
+        }
+    }
+    RTM_CUDA(cudaStreamSynchronize(P->stream));
+    return RTM_OK;
+}
+
+static int one_step(rtm_plan *P, int flags, bool with_psi)
+{
+    StepArgs<float> a;
+    fill_common<float>(P, a);
+    a.u_next = P->at<float>(P->L.u[1]);
+    a.flags = flags;
+    if (with_psi) {
+        PsiArgs<float> q;
+        fill_psi<float>(P, a, q);
+        q.u = P->at<float>(P->L.u[0]);
+        RTM_CUDA(launch_psi<float>(q, P->stream));
+        P->launches++;
+    }
+    RTM_CUDA(launch_step<float>(0, &P->tm_u[0], &P->tm_u[0], a, P->stream));
+    P->launches++;
+    return check_status(P);
+}
+
+}  // namespace rtm
+
+extern "C" {
+
+int rtm_iso_acoustic_wave_equation(const rtm_params *p, const float *pond, const float *wave2,
+                                   float *wave3)
+{
+    if (!p || !pond || !wave2 || !wave3) return fail(RTM_ERR_INVALID, "null argument");
+    rtm_plan *P = nullptr;
+    RTM_TRY(step_plan(p, &P));
+    int st = field_from_host(P, P->at<float>(P->L.coef), pond);
+    if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[0]), wave2);
+    if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[1]), wave3);
+    if (st == RTM_OK) st = one_step(P, F_NO_CPML, false);
+    if (st == RTM_OK) st = field_to_host(P, wave3, P->at<float>(P->L.u[1]));
+    release_plan(P);
+    return st;
+}
+
+int rtm_aiso_attenuation_cpml(const rtm_params *p, const float *wave1, float *wave2,
+                              const float *coef, const float *a_left, const float *b_left,
+                              const float *a_right, const float *b_right, const float *a_top,
+                              const float *b_top, const float *a_bottom, const float *b_bottom,
+                              float *psi_left, float *psi_right, float *psi_top,
+                              float *psi_bottom, float *xi_left, float *xi_right, float *xi_top,
+                              float *xi_bottom)
+{
+    if (!p || !wave1 || !wave2 || !coef) return fail(RTM_ERR_INVALID, "null argument");
+    rtm_plan *P = nullptr;
+    RTM_TRY(step_plan(p, &P));
+    const Geom &g = P->g;
+    int st = field_from_host(P, P->at<float>(P->L.coef), coef);
+    if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[0]), wave1);
+    if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[1]), wave2);
+    float *strips[8] = {psi_left, psi_right, psi_top, psi_bottom, xi_left, xi_right, xi_top, xi_bottom};
+    if (st == RTM_OK) st = strips_io(P, 1, strips);
+    // caller-supplied profiles for this call; the plan's own are restored afterwards
+    std::vector<float> prof(P->h_prof.size());
+    {
+        float *d = prof.data();
+        const float *src[8] = {a_left, b_left, a_right, b_right, a_top, b_top, a_bottom, b_bottom};
+        const int n[8] = {g.thl, g.thl, g.thr, g.thr, g.thu, g.thu, g.thd, g.thd};
+        for (int i = 0; i < 8; ++i) { memcpy(d, src[i], n[i] * sizeof(float)); d += n[i]; }
+    }
+    if (st == RTM_OK && cudaMemcpy(P->base + P->L.prof, prof.data(), prof.size() * sizeof(float),
+                                   cudaMemcpyHostToDevice) != cudaSuccess)
+        st = fail(RTM_ERR_CUDA, "profile upload");
+    if (st == RTM_OK) st = one_step(P, F_NO_STENCIL, true);
+    if (st == RTM_OK) st = field_to_host(P, wave2, P->at<float>(P->L.u[1]));
+    if (st == RTM_OK) st = strips_io(P, 0, strips);
+    cudaMemcpy(P->base + P->L.prof, P->h_prof.data(), P->h_prof.size() * sizeof(float),
+               cudaMemcpyHostToDevice);
+    release_plan(P);
+    return st;
+}
+
+int rtm_normalized_cross_correlation(const rtm_params *p, float *image, float *self_image,
+                                     const float *source, const float *receiver)
+{
+    if (!p || !image || !self_image || !source || !receiver) return fail(RTM_ERR_INVALID, "null argument");
+    rtm_plan *P = nullptr;
+    RTM_TRY(step_plan(p, &P));
+    const Geom &g = P->g;
+    const size_t n = (size_t)g.nx * g.nz;
+    int st = field_from_host(P, P->at<float>(P->L.u[0]), source);
+    if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.r[0]), receiver);
+    float *stage = P->at<float>(P->L.staging);
+    if (st == RTM_OK) {
+        cudaMemsetAsync(P->base + P->L.img, 0, sizeof(double) * (size_t)g.nx * g.pitch, P->stream);
+        cudaMemsetAsync(P->base + P->L.slf, 0, sizeof(double) * (size_t)g.nx * g.pitch, P->stream);
+        if (launch_xcorr<float>(g, P->at<float>(P->L.u[0]), P->at<float>(P->L.r[0]),
+                                P->at<double>(P->L.img), P->at<double>(P->L.slf), P->stream) != cudaSuccess)
+            st = fail(RTM_ERR_CUDA, "xcorr launch");
+        P->image_valid = true;
+        P->launches++;
+    }
+    if (st == RTM_OK) st = upload_host(P, stage, image, n * sizeof(float));
+    if (st == RTM_OK) st = image_to(P, 0, stage, 0, 1);
+    if (st == RTM_OK && cudaMemcpyAsync(image, stage, n * sizeof(float), cudaMemcpyDeviceToHost, P->stream) != cudaSuccess)
+        st = fail(RTM_ERR_CUDA, "image download");
+    if (st == RTM_OK) st = upload_host(P, stage, self_image, n * sizeof(float));
+    if (st == RTM_OK) st = image_to(P, 1, stage, 0, 1);
+    if (st == RTM_OK && cudaMemcpyAsync(self_image, stage, n * sizeof(float), cudaMemcpyDeviceToHost, P->stream) != cudaSuccess)
+        st = fail(RTM_ERR_CUDA, "image download");
+    if (st == RTM_OK) st = check_status(P);
+    P->image_valid = false;
+    release_plan(P);
+    return st;
+}
+
+int rtm_laplacian_filter2D(const rtm_params *p, float *lp, const float *image)
+{
+    if (!p || !lp || !image) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->nx < 1 || p->nz < 1) return fail(RTM_ERR_INVALID, "empty image");
+    const size_t n = (size_t)p->nx * p->nz;
+    float *d = nullptr;
+    if (cudaMalloc(&d, 2 * n * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(RTM_ERR_NOMEM, "laplacian buffers");
+    }
+    int st = RTM_OK;
+    if (cudaMemcpy(d, image, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        launch_laplacian(p->nx, p->nz, d, d + n, 0) != cudaSuccess)
+        st = fail(RTM_ERR_CUDA, "laplacian");
+    // only the cells the reference writes: [4, nx-4) x [4, nz-4) (math_functions.c:11-14)
+    if (st == RTM_OK && p->nx > 8 && p->nz > 8 &&
+        cudaMemcpy2D(lp + 4 * (size_t)p->nz + 4, p->nz * sizeof(float), d + n + 4 * (size_t)p->nz + 4,
+                     p->nz * sizeof(float), (p->nz - 8) * sizeof(float), p->nx - 8,
+                     cudaMemcpyDeviceToHost) != cudaSuccess)
+        st = fail(RTM_ERR_CUDA, "laplacian download");
+    cudaFree(d);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+"""CUDA engine vs the oracle / the reference's own outputs, through the C ABI.
+
+Tolerances (relative L2 over the whole array):
+  one step (stencil, CPML)           <= 1e-6   (FMA contraction is the only difference)
+  wavefields / seismograms after nt  <= 1e-5
+  images, snapshot storage           <= 1e-4   (the stated bar for the FP32 path)
+  images, ring reconstruction        <= 1e-4
+  FP64 engine vs FP64 oracle         <= 1e-10
+"""
+import numpy as np
+import pytest
+
+from golden_util import case_params, load, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+CASES = ("uneven", "quirks")
+
+
+def _params(eng, d, name, **kw):
+    p = eng.RtmParams.make(**case_params(d, name))
+    return p.replace(**kw)
+
+
+def test_step_stencil_matches_reference_kat(engine):
+    d = load()
+    p = _params(engine, d, "uneven")
+    out = engine.iso_acoustic_wave_equation(p, d["kat/coef"], d["kat/u1"], d["kat/u2"])
+    assert rel_l2(out, d["kat/stencil"]) <= 1e-6
+    # cells the reference never writes (outer 4-cell frame) are untouched
+    assert np.array_equal(out[:4], d["kat/u2"][:4]) and np.array_equal(out[:, -4:], d["kat/u2"][:, -4:])
+
+
+def test_step_cpml_matches_reference_kat(engine):
+    d = load()
+    p = _params(engine, d, "uneven")
+    psi = {k: d["kat/psi_in_" + k].copy() for k in "lrtb"}
+    xi = {k: d["kat/xi_in_" + k].copy() for k in "lrtb"}
+    prof = engine.attenuation_profile_cpml(p)
+    out = engine.aiso_attenuation_cpml(p, d["kat/u1"], d["kat/u2"], d["kat/coef"], prof, psi, xi)
+    assert rel_l2(out, d["kat/cpml"]) <= 1e-6
+    for k in "lrtb":
+        assert rel_l2(psi[k], d["kat/psi_out_" + k]) <= 1e-6, k
+        assert rel_l2(xi[k], d["kat/xi_out_" + k]) <= 1e-6, k
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("storage", (0, 1))
+def test_migration_matches_reference(engine, name, storage):
+    d = load()
+    p = _params(engine, d, name, storage=storage)
+    if storage == 1:
+        try:
+            engine.params_check(p)
+        except engine.RtmError:
+            pytest.skip("shot outside the reconstruction region for this case")
+    img, slf = engine.migrate_shot(p, d[name + "/ext"], d[name + "/wavelet"], d[name + "/seis"])
+    assert np.abs(img).max() > 0
+    assert rel_l2(img, d[name + "/image"]) <= 1e-4
+    assert rel_l2(slf, d[name + "/self"]) <= 1e-4
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_forward_final_fields_and_recording_match_oracle(engine, oracle, name):
+    import torch
+    d = load()
+    p = _params(engine, d, name, storage=0)
+    ext, wav = d[name + "/ext"], d[name + "/wavelet"]
+    ref = oracle.forward(p.as_dict(), ext, wav, snapshots=False, record=True)
+    plan = engine.Plan(p)
+    dv = torch.from_numpy(ext).cuda()
+    dw = torch.from_numpy(wav).cuda()
+    seis = torch.zeros((p.rec_count, p.nt), dtype=torch.float32, device="cuda")
+    plan.forward(dv, dw, seis)
+    plan.sync()
+    last = torch.empty((p.dim_x, p.dim_z), dtype=torch.float32, device="cuda")
+    prev = torch.empty_like(last)
+    plan.read_field(0, last)
+    plan.read_field(1, prev)
+    assert rel_l2(last.cpu().numpy(), ref["u_last"]) <= 1e-5
+    assert rel_l2(prev.cpu().numpy(), ref["u_prev"]) <= 1e-5
+    assert rel_l2(seis.cpu().numpy(), ref["seis"]) <= 1e-5
+    plan.close()
+
+
+def test_model_seismogram_host_entry_point(engine, oracle):
+    d = load()
+    p = _params(engine, d, "uneven")
+    true = d["uneven/ext"] * np.float32(1.04)
+    seis = engine.model_seismogram(p, true, d["uneven/wavelet"])
+    assert rel_l2(seis, d["uneven/seis"]) <= 1e-5
+
+
+def test_sim_id_forward_then_adjoint(engine):
+    d = load()
+    p = _params(engine, d, "uneven", storage=1)
+    shot = (p.shot_x, p.shot_z)
+    engine.forward_modeling(p, 3, shot, d["uneven/ext"], d["uneven/wavelet"])
+    engine.forward_modeling(p, 4, shot, d["uneven/ext"], d["uneven/wavelet"])
+    img = np.zeros((p.nx, p.nz), np.float32)
+    slf = np.zeros((p.nx, p.nz), np.float32)
+    engine.adjoint_modeling(p, 4, shot, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"], img, slf)
+    engine.adjoint_modeling(p, 3, shot, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"], img, slf)
+    # two identical shots accumulated into the same buffers
+    assert rel_l2(img, 2 * d["uneven/image"]) <= 1e-4
+    with pytest.raises(engine.RtmError) as e:
+        engine.adjoint_modeling(p, 3, shot, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"], img, slf)
+    assert e.value.status == 4   # RTM_ERR_STATE: the state of sim 3 was consumed
+
+
+@pytest.mark.parametrize("storage", (0, 1))
+def test_fp64_engine_matches_fp64_oracle(engine, oracle, storage):
+    import torch
+    d = load()
+    name = "uneven"
+    p = _params(engine, d, name, storage=storage, compute=1)
+    ext, wav, seis = d[name + "/ext"], d[name + "/wavelet"], d[name + "/seis"]
+    ref_img, ref_slf = oracle.migrate(p.as_dict(), ext, wav, seis, dtype=np.float64)
+    plan = engine.Plan(p)
+    plan.forward(torch.from_numpy(ext).cuda(), torch.from_numpy(wav).cuda())
+    plan.adjoint(torch.from_numpy(seis).cuda())
+    img = torch.empty((p.nx, p.nz), dtype=torch.float64, device="cuda")
+    slf = torch.empty_like(img)
+    plan.read_image(0, img, as_double=True)
+    plan.read_image(1, slf, as_double=True)
+    plan.sync()
+    tol = 1e-10 if storage == 0 else 1e-8
+    assert rel_l2(img.cpu().numpy(), ref_img) <= tol
+    assert rel_l2(slf.cpu().numpy(), ref_slf) <= tol
+    plan.close()
+
+
+def test_laplacian_and_xcorr_drop_ins(engine, oracle):
+    d = load()
+    p = _params(engine, d, "uneven")
+    lp = engine.laplacian_filter2D(p, d["kat/lap_in"])
+    assert rel_l2(lp, d["kat/lap_out"]) <= 1e-6
+    assert np.all(lp[:4] == 0) and np.all(lp[:, -4:] == 0)
+    img = np.full((p.nx, p.nz), 0.5, np.float32)
+    slf = np.zeros((p.nx, p.nz), np.float32)
+    s, r = d["kat/u1"], d["kat/u2"]
+    engine.normalized_cross_correlation(p, img, slf, s, r)
+    ri, rs = np.full((p.nx, p.nz), 0.5, np.float32), np.zeros((p.nx, p.nz), np.float32)
+    oracle.xcorr(p.as_dict(), ri, rs, s, r)
+    assert rel_l2(img, ri) <= 1e-6 and rel_l2(slf, rs) <= 1e-6
+
+
+@pytest.mark.parametrize("tile_x", (8, 16, 32))
+def test_tile_widths_agree(engine, tile_x):
+    d = load()
+    p = _params(engine, d, "uneven", storage=1, tile_x=tile_x)
+    img, _ = engine.migrate_shot(p, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"])
+    assert rel_l2(img, d["uneven/image"]) <= 1e-4
+
+
+def test_small_workload_against_oracle(engine, oracle):
+    """The 400 x 200, nt = 2000 plain workload: ring and snapshot storage vs the oracle."""
+    from rtmuq2d_gb300 import workloads
+    p = workloads.params_small()
+    true, mig = workloads.models_small(p, seed=0)
+    wav = workloads.wavelet_for(p)
+    ext_true = engine.extend_matrix(p, true)
+    ext = engine.extend_matrix(p, mig)
+    seis = oracle.model_seismogram(p.as_dict(), ext_true, wav)
+    ref_img, ref_slf = oracle.migrate(p.as_dict(), ext, wav, seis)
+    for storage in (0, 1):
+        img, slf = engine.migrate_shot(p.replace(storage=storage), ext, wav, seis)
+        assert rel_l2(img, ref_img) <= 1e-4, storage
+        assert rel_l2(slf, ref_slf) <= 1e-4, storage
