@@ -196,21 +196,6 @@ __device__ __forceinline__ T lap8(const T (&W)[9][4], const T (&zz)[12], int j)
         + (T)RTM_AC4 * (((W[0][j] + W[8][j]) + zz[0 + j]) + zz[8 + j]);
 }
 
-// 1-D second derivative used by the CPML (absorbingBoundaryCondition.c:208-212 order).
-template <typename T>
-__device__ __forceinline__ T d2x(const T (&W)[9][4], int j)
-{
-    return (T)RTM_AC4 * (W[8][j] + W[0][j]) + (T)RTM_AC3 * (W[7][j] + W[1][j])
-         + (T)RTM_AC2 * (W[6][j] + W[2][j]) + (T)RTM_AC1 * (W[5][j] + W[3][j])
-         + (T)RTM_AC0 * W[4][j];
-}
-template <typename T>
-__device__ __forceinline__ T d2z(const T (&zz)[12], int j)
-{
-    return (T)RTM_AC4 * (zz[8 + j] + zz[j]) + (T)RTM_AC3 * (zz[7 + j] + zz[1 + j])
-         + (T)RTM_AC2 * (zz[6 + j] + zz[2 + j]) + (T)RTM_AC1 * (zz[5 + j] + zz[3 + j])
-         + (T)RTM_AC0 * zz[4 + j];
-}
 // First derivative along a strided line (B coefficients, :183-186 order).
 template <typename T>
 __device__ __forceinline__ T d1(const T *f, ptrdiff_t s)
@@ -233,289 +218,7 @@ __device__ __forceinline__ float block_max(float v, float *red)
     return m;
 }
 
-// ---- the fused step kernel -----------------------------------------------------------------
-template <typename T, int BWD, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_s,
-           const StepArgs<T> a)
-{
-    constexpr int RX = 4;
-    constexpr int TXC = WARPS * RX;
-    constexpr int SXC = TXC + 2 * HALO;
-    constexpr int TILE = SXC * SZ;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    T *su = reinterpret_cast<T *>(smem_raw);
-    T *ss = su + TILE;
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ float red[WARPS];
-
-    const Geom &g = a.g;
-    const int x0 = blockIdx.x * TXC;
-    const int z0 = blockIdx.y * TZ;
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const bool recon = BWD && (a.flags & F_RECON);
-
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t bytes = (uint32_t)(TILE * sizeof(T)) * (recon ? 2u : 1u);
-        mbar_arrive_expect_tx(&bar, bytes);
-        tma_load_2d(su, &tm_u, z0 - HALO, x0 - HALO, &bar);
-        if (recon) tma_load_2d(ss, &tm_s, z0 - HALO, x0 - HALO, &bar);
-    }
-
-    const int zq = z0 + 4 * lane;          // first z of this thread's quad
-    const int xb = x0 + warp * RX;         // first x column of this thread
-    const bool zok = zq < g.dimz;
-    const size_t P = (size_t)g.pitch;
-
-    // Per-cell inputs with no reuse go straight to registers while the TMA is in flight.
-    T prv[RX][4], cf[RX][4];
-#pragma unroll
-    for (int r = 0; r < RX; ++r) {
-        const int x = xb + r;
-        if (zok && x < g.dimx) {
-            ld4(a.u_next + (size_t)x * P + zq, prv[r]);
-            ldg4(a.coef + (size_t)x * P + zq, cf[r]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) { prv[r][j] = (T)0; cf[r][j] = (T)0; }
-        }
-    }
-
-    const bool ok = mbar_wait_bounded(&bar, 0, 2000000000ull);
-    if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) atomicOr(a.status, ST_TMA_TIMEOUT);
-        mbar_wait_bounded(&bar, 0, 2000000000ull);   // let copies in flight land
-        return;
-    }
-
-    const T h1 = a.h1, h2 = a.h2, h3 = a.h3;
-    const int row0 = warp * RX;             // tile row of column xb-4
-    const int zi = 4 * lane + HALO;         // tile index of the quad's first cell
-    const bool cpml_tile = !(a.flags & F_NO_CPML) &&
-                           ((x0 < g.thl - 4) || (x0 + TXC > g.dimx - g.thr + 4) ||
-                            (z0 < g.thu - 4) || (z0 + TZ > g.dimz - g.thd + 4));
-    const bool stencil = !(a.flags & F_NO_STENCIL);
-
-    // ---------------- the propagated field (source field forward, receiver field backward)
-    T un[RX][4];
-    {
-        T W[9][4];
-#pragma unroll
-        for (int m = 0; m < 8; ++m) ld4(su + (row0 + m) * SZ + zi, W[m]);
-#pragma unroll
-        for (int r = 0; r < RX; ++r) {
-            ld4(su + (row0 + r + 8) * SZ + zi, W[8]);
-            T zz[12];
-            {
-                T zm[4], zp[4];
-                ld4(su + (row0 + r + 4) * SZ + zi - 4, zm);
-                ld4(su + (row0 + r + 4) * SZ + zi + 4, zp);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) { zz[j] = zm[j]; zz[4 + j] = W[4][j]; zz[8 + j] = zp[j]; }
-            }
-            const int x = xb + r;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int z = zq + j;
-                T v = prv[r][j];
-                if (x < g.dimx && z < g.dimz) {
-                    if (stencil && x >= 4 && x < g.dimx - 4 && z >= 4 && z < g.dimz - 4)
-                        v = cf[r][j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - prv[r][j];
-                    if (cpml_tile) {
-                        const T ch2 = cf[r][j] * h2;
-                        if (x >= 4 && x < g.thl - 4 && z >= 4 && z < g.dimz - 4) {
-                            const size_t at = (size_t)x * P + z;
-                            const T dpsi = d1<T>(a.psi_l + at, (ptrdiff_t)P) * h1;
-                            const T xi = (T)a.b_l[x] * a.xi_l[at] +
-                                         (T)a.a_l[x] * (d2x<T>(W, j) * h3 + dpsi);
-                            a.xi_l[at] = xi;
-                            v = v + ch2 * (dpsi + xi);
-                        }
-                        if (z >= 4 && z < g.thu - 4) {
-                            const size_t at = (size_t)x * g.st + z;
-                            const T dpsi = d1<T>(a.psi_t + at, 1) * h1;
-                            const T xi = (T)a.b_t[z] * a.xi_t[at] +
-                                         (T)a.a_t[z] * (d2z<T>(zz, j) * h3 + dpsi);
-                            a.xi_t[at] = xi;
-                            v = v + ch2 * (dpsi + xi);
-                        }
-                        if (x >= g.dimx - g.thr + 4 && x < g.dimx - 4 && z >= 4 && z < g.dimz - 4) {
-                            const int li = x - (g.dimx - g.thr);
-                            const size_t at = (size_t)li * P + z;
-                            const T dpsi = d1<T>(a.psi_r + at, (ptrdiff_t)P) * h1;
-                            const T xi = (T)a.b_r[li] * a.xi_r[at] +
-                                         (T)a.a_r[li] * (d2x<T>(W, j) * h3 + dpsi);
-                            a.xi_r[at] = xi;
-                            v = v + ch2 * (dpsi + xi);
-                        }
-                        if (x >= 4 && x < g.dimx - 4 && z >= g.dimz - g.thd + 4 && z < g.dimz - 4) {
-                            const int lz = z - (g.dimz - g.thd);
-                            const size_t at = (size_t)x * g.sb + lz;
-                            const T dpsi = d1<T>(a.psi_b + at, 1) * h1;
-                            const T xi = (T)a.b_b[lz] * a.xi_b[at] +
-                                         (T)a.a_b[lz] * (d2z<T>(zz, j) * h3 + dpsi);
-                            a.xi_b[at] = xi;
-                            v = v + ch2 * (dpsi + xi);
-                        }
-                    }
-                    if (!BWD) {
-                        if ((a.flags & F_SRC) && x == g.xs && z == g.zs) {
-                            if (sizeof(T) == sizeof(float))
-                                v = v + (T)(a.wavelet[a.t] * (float)cf[r][j]);
-                            else
-                                v = v + (T)a.wavelet[a.t] * cf[r][j];
-                        }
-                        if ((a.flags & F_RECORD) && z == g.zrec) {
-                            const int n = a.rec_cnt[x];
-                            const int f = a.rec_first[x];
-                            for (int q = 0; q < n; ++q)
-                                a.rec_out[(size_t)(f + q) * g.nt + a.t] = v;
-                        }
-                    } else {
-                        if ((a.flags & F_OVERWRITE) && z == g.zrec) {
-                            const int q = a.rec_last[x];
-                            if (q >= 0) v = (T)a.seis_row[q];
-                        }
-                    }
-                }
-                un[r][j] = v;
-            }
-#pragma unroll
-            for (int m = 0; m < 8; ++m)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
-        }
-    }
-
-    // ---------------- forward: storage of the source wavefield
-    if (!BWD && (a.flags & (F_RING_SAVE | F_SNAP_SAVE))) {
-        const bool ring = a.flags & F_RING_SAVE;
-        float inv_scale = 1.0f;
-        if (a.store_prec != 0) {            // 16-bit: per-step, per-tile max-abs scale
-            float mx = 0.0f;
-#pragma unroll
-            for (int r = 0; r < RX; ++r)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int x = xb + r, z = zq + j;
-                    if (x < g.dimx && z < g.dimz &&
-                        (ring ? ring_index(g, x, z) >= 0 : in_interior(g, x, z)))
-                        mx = fmaxf(mx, fabsf((float)un[r][j]));
-                }
-            mx = block_max<WARPS>(mx, red);
-            const float target = a.store_prec == 2 ? kFp16Target : kBf16Target;
-            const float scale = mx > 0.0f ? mx / target : 1.0f;
-            inv_scale = mx > 0.0f ? target / mx : 1.0f;
-            if (threadIdx.x == 0) a.store_scale[blockIdx.y * gridDim.x + blockIdx.x] = scale;
-        }
-#pragma unroll
-        for (int r = 0; r < RX; ++r)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int x = xb + r, z = zq + j;
-                if (x >= g.dimx || z >= g.dimz) continue;
-                if (ring) {
-                    const int idx = ring_index(g, x, z);
-                    if (idx >= 0) store_put<T>(a.store, a.store_prec, (size_t)idx, un[r][j], inv_scale);
-                } else if (in_interior(g, x, z)) {
-                    store_put<T>(a.store, a.store_prec, (size_t)(x - g.thl) * P + z, un[r][j],
-                                 inv_scale);
-                }
-            }
-    }
-
-    // ---------------- write the propagated field
-#pragma unroll
-    for (int r = 0; r < RX; ++r) {
-        const int x = xb + r;
-        if (zok && x < g.dimx) st4(a.u_next + (size_t)x * P + zq, un[r]);
-    }
-
-    if (!BWD) return;
-
-    // ---------------- backward: source-field reconstruction and imaging
-    const bool image = a.flags & F_IMAGE;
-    if (!recon && !image) return;
-    const float tile_scale =
-        (recon && a.store_prec != 0) ? a.store_scale[blockIdx.y * gridDim.x + blockIdx.x] : 1.0f;
-    const int tsrc = g.nt + 1 - a.t;        // forward step whose source term is undone
-    T W[9][4];
-    if (recon) {
-#pragma unroll
-        for (int m = 0; m < 8; ++m) ld4(ss + (row0 + m) * SZ + zi, W[m]);
-    }
-#pragma unroll
-    for (int r = 0; r < RX; ++r) {
-        const int x = xb + r;
-        T s[4] = {(T)0, (T)0, (T)0, (T)0};
-        if (recon) {
-            ld4(ss + (row0 + r + 8) * SZ + zi, W[8]);
-            T zz[12];
-            {
-                T zm[4], zp[4];
-                ld4(ss + (row0 + r + 4) * SZ + zi - 4, zm);
-                ld4(ss + (row0 + r + 4) * SZ + zi + 4, zp);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) { zz[j] = zm[j]; zz[4 + j] = W[4][j]; zz[8 + j] = zp[j]; }
-            }
-            T sp[4];
-            if (zok && x < g.dimx) ld4(a.s_next + (size_t)x * P + zq, sp);
-            else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) sp[j] = (T)0;
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int z = zq + j;
-                T v = sp[j];
-                if (x < g.dimx && z < g.dimz) {
-                    if (in_region(g, x, z)) {
-                        v = cf[r][j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - sp[j];
-                        if ((a.flags & F_RECON_SRC) && x == g.xs && z == g.zs) {
-                            if (sizeof(T) == sizeof(float))
-                                v = v + (T)(a.wavelet[tsrc] * (float)cf[r][j]);
-                            else
-                                v = v + (T)a.wavelet[tsrc] * cf[r][j];
-                        }
-                    } else {
-                        const int idx = ring_index(g, x, z);
-                        if (idx >= 0) v = store_get<T>(a.store, a.store_prec, (size_t)idx, tile_scale);
-                    }
-                }
-                s[j] = v;
-            }
-            if (zok && x < g.dimx) st4(a.s_next + (size_t)x * P + zq, s);
-#pragma unroll
-            for (int m = 0; m < 8; ++m)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
-        }
-        if (image) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int z = zq + j;
-                if (x < g.dimx && z < g.dimz && in_interior(g, x, z)) {
-                    const size_t o = (size_t)(x - g.thl) * P + z;
-                    double sv;
-                    if (recon) sv = (double)s[j];
-                    else if (a.flags & F_IMAGE_SNAP)
-                        sv = (double)store_get<T>(a.s_snap, a.store_prec, o, a.store_scale ?
-                                                  a.store_scale[blockIdx.y * gridDim.x + blockIdx.x] : 1.0f);
-                    else sv = (double)a.s_fixed[(size_t)x * P + z];
-                    const double rv = (double)un[r][j];
-                    a.img[o] += sv * rv;
-                    a.slf[o] += sv * sv;
-                }
-            }
-        }
-    }
-}
+#include "rtm_step.cuh"
 
 // ---- CPML psi update (runs before k_step) -------------------------------------------------
 template <typename T>
@@ -663,12 +366,12 @@ template <typename T, int BWD, int WARPS>
 static cudaError_t launch_step_w(const CUtensorMap *tm_u, const CUtensorMap *tm_s,
                                  const StepArgs<T> &a, cudaStream_t s)
 {
-    const size_t smem = step_smem_bytes(BWD, sizeof(T), WARPS * 4);
+    const size_t smem = step_smem_bytes(BWD, sizeof(T), StepCfg<T, WARPS>::TXC);
     static bool configured = false;   // attribute set once per instantiation
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(k_step<T, BWD, WARPS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)step_smem_bytes(BWD, sizeof(T), WARPS * 4));
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
@@ -681,19 +384,19 @@ template <typename T>
 cudaError_t launch_step(int backward, const CUtensorMap *tm_u, const CUtensorMap *tm_s,
                         const StepArgs<T> &a, cudaStream_t s)
 {
-    const int warps = a.g.tx / 4;
+    const int warps = a.g.tx / StepCfg<T, 4>::RXC;
     if (backward) {
         switch (warps) {
-        case 2: return launch_step_w<T, 1, 2>(tm_u, tm_s, a, s);
         case 4: return launch_step_w<T, 1, 4>(tm_u, tm_s, a, s);
         case 8: return launch_step_w<T, 1, 8>(tm_u, tm_s, a, s);
+        case 16: return launch_step_w<T, 1, 16>(tm_u, tm_s, a, s);
         default: return cudaErrorInvalidValue;
         }
     }
     switch (warps) {
-    case 2: return launch_step_w<T, 0, 2>(tm_u, tm_s, a, s);
     case 4: return launch_step_w<T, 0, 4>(tm_u, tm_s, a, s);
     case 8: return launch_step_w<T, 0, 8>(tm_u, tm_s, a, s);
+    case 16: return launch_step_w<T, 0, 16>(tm_u, tm_s, a, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -167,3 +167,18 @@ def test_small_workload_against_oracle(engine, oracle):
         img, slf = engine.migrate_shot(p.replace(storage=storage), ext, wav, seis)
         assert rel_l2(img, ref_img) <= 1e-4, storage
         assert rel_l2(slf, ref_slf) <= 1e-4, storage
+
+
+@pytest.mark.parametrize("storage", (0, 1))
+@pytest.mark.parametrize("precision,tol", ((1, 5e-2), (2, 5e-3)))
+def test_16bit_storage_close_to_fp32(engine, storage, precision, tol):
+    """BF16 / FP16 storage of the source wavefield with per-step, per-tile max-abs scales:
+    the image stays close to the FP32-storage image (stencil and CPML stay FP32)."""
+    d = load()
+    p = _params(engine, d, "uneven", storage=storage)
+    ref, _ = engine.migrate_shot(p, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"])
+    img, _ = engine.migrate_shot(p.replace(precision=precision), d["uneven/ext"], d["uneven/wavelet"],
+                                 d["uneven/seis"])
+    err = rel_l2(img, ref)
+    assert err <= tol, err
+    assert err > 0.0          # the 16-bit path really ran
