@@ -188,6 +188,28 @@ int rtm_plan_profile_read(rtm_plan *plan, double *fwd_ms, int *fwd_n, double *bw
 /* Frees the plans the host-buffer entry points keep for reuse. */
 void rtm_release_cached(void);
 
+/* ---- migration without device allocation -------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc: a host whose
+ * device memory is owned by another allocator or held to a fixed budget, or a serving loop
+ * that cannot take the implicit device synchronisation of an allocation between requests.
+ * Same work and results as rtm_plan_create + rtm_plan_forward + rtm_plan_adjoint (device
+ * pointers, reference layouts, image and self image written, not accumulated), but every
+ * scratch buffer (wavefields, CPML strips, source-wavefield store, transposed seismogram,
+ * FP64 image accumulators) lives in one static 64 MiB device array inside the library; no
+ * cudaMalloc, cudaFree or other allocating call is made.  Every GPU that loads the library
+ * holds those 64 MiB until the process exits.
+ * Limit: a configuration whose footprint (rtm_footprint_bytes) exceeds 64 MiB, or with a
+ * CPML thicker than 512 cells, is rejected with RTM_ERR_INVALID and a message naming the
+ * bytes needed -- e.g. a 400 x 200 model with nt = 2000 and ring storage fits (~52 MB).
+ * The first call on each device looks up the array's device address (cudaGetSymbolAddress,
+ * with that device current); make that first call before any stream capture.
+ * All calls on a device share the array and each call rebuilds what it needs, so calls run
+ * one at a time: calls that overlap on the GPU (other streams, other host threads) race.
+ * stream: cudaStream_t to run on (NULL = default stream); the call returns when done. */
+int rtm_migrate_shot_static(const rtm_params *p, const void *d_velocity, const void *d_wavelet,
+                            const void *d_seismogram, void *d_image, void *d_self_image,
+                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1117,3 +1117,113 @@ int rtm_laplacian_filter2D(const rtm_params *p, float *lp, const float *image)
 }
 
 }  // extern "C"
+
+// ---- single-shot migration without device allocation --------------------------------------
+// Scratch of rtm_migrate_shot_static: the wavefields, CPML strips, source-wavefield store,
+// transposed seismogram and FP64 image accumulators of one migration live in this
+// file-scope array instead of a cudaMalloc'd plan.  Every GPU that loads the library holds
+// these 64 MiB until the process exits.  All calls on a device share it.
+#define RTM_STATIC_SCRATCH_BYTES (64ull << 20)
+#define RTM_STATIC_MAX_THICK 512
+static __device__ __align__(256) unsigned char g_static_scratch[RTM_STATIC_SCRATCH_BYTES];
+
+namespace rtm {
+
+// Receiver column maps on the device (same maps plan_alloc builds on the host).
+__global__ void k_rec_maps(Geom g, int rec_first, int rec_spacing, int rec_count, int *last,
+                           int *first, int *cnt)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= g.dimx) return;
+    const int c0 = g.thl + rec_first;                    // column of receiver 0
+    const int step = rec_spacing - 1;                    // backward_modeling.c:279
+    int l = -1, f = -1, n = 0;
+    if (rec_count > 0) {
+        if (step == 0) {
+            if (x == c0) { l = rec_count - 1; f = 0; n = rec_count; }
+        } else if ((x - c0) % step == 0) {
+            const int i = (x - c0) / step;
+            if (i >= 0 && i < rec_count) { l = i; f = i; n = 1; }
+        }
+    }
+    last[x] = l;
+    first[x] = f;
+    cnt[x] = n;
+}
+
+static std::mutex g_static_mu;
+static void *g_static_ptr[256];
+
+// Device address of the static scratch on device `dev` (looked up once per device, with
+// that device current).
+static int static_scratch(int dev, void **out)
+{
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (dev < 0 || dev >= 256) return fail(RTM_ERR_INVALID, "device ordinal %d out of range", dev);
+    if (!g_static_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(RTM_ERR_CUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return RTM_OK;
+}
+
+}  // namespace rtm
+
+extern "C" int rtm_migrate_shot_static(const rtm_params *p, const void *d_velocity,
+                                       const void *d_wavelet, const void *d_seismogram,
+                                       void *d_image, void *d_self_image, void *stream)
+{
+    if (!p || !d_velocity || !d_image || !d_self_image) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->n_wavelet > 0 && !d_wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
+    if (p->rec_count > 0 && !d_seismogram) return fail(RTM_ERR_INVALID, "null seismogram");
+    RTM_TRY(check_params(*p));
+    if (p->th_left > RTM_STATIC_MAX_THICK || p->th_right > RTM_STATIC_MAX_THICK ||
+        p->th_up > RTM_STATIC_MAX_THICK || p->th_down > RTM_STATIC_MAX_THICK)
+        return fail(RTM_ERR_INVALID, "CPML thicker than %d cells", RTM_STATIC_MAX_THICK);
+    const Geom g = make_geom(*p);
+    const Layout L = make_layout(*p, g);
+    if (L.total > RTM_STATIC_SCRATCH_BYTES)
+        return fail(RTM_ERR_INVALID,
+                    "this migration needs %zu bytes of scratch; the static array holds %llu bytes",
+                    L.total, (unsigned long long)RTM_STATIC_SCRATCH_BYTES);
+    int dev = 0;
+    RTM_CUDA(cudaGetDevice(&dev));
+    void *base = nullptr;
+    RTM_TRY(static_scratch(dev, &base));
+
+    rtm_plan P;                                   // host-side view over the static scratch
+    P.p = *p;
+    P.g = g;
+    P.L = L;
+    P.es = p->compute == RTM_COMPUTE_FP64 ? 8 : 4;
+    P.base = static_cast<unsigned char *>(base);
+    P.stream = static_cast<cudaStream_t>(stream);
+    P.own_stream = false;
+    for (int i = 0; i < 2; ++i) {
+        RTM_TRY(make_field_map(&P.tm_u[i], P.base + L.u[i], g, P.es));
+        RTM_TRY(make_field_map(&P.tm_r[i], P.base + L.r[i], g, P.es));
+    }
+    // what the previous call left in the array: status word and receiver maps are rebuilt;
+    // fields, strips and accumulators are zeroed by the forward / adjoint drivers
+    RTM_CUDA(cudaMemsetAsync(P.base + L.status, 0, 256, P.stream));
+    float prof[8 * RTM_STATIC_MAX_THICK];
+    float *a_l = prof, *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
+    float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
+    rtm_attenuation_profile_cpml(p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
+    RTM_CUDA(cudaMemcpyAsync(P.base + L.prof, prof, sizeof(float) * 2 * (size_t)(g.thl + g.thr + g.thu + g.thd),
+                             cudaMemcpyHostToDevice, P.stream));
+    int *rec = P.at<int>(L.rec);
+    k_rec_maps<<<(g.dimx + 127) / 128, 128, 0, P.stream>>>(g, p->rec_first, p->rec_spacing, p->rec_count,
+                                                            rec, rec + g.dimx, rec + 2 * g.dimx);
+    RTM_CUDA(cudaGetLastError());
+    RTM_TRY(dispatch_forward(&P, static_cast<const float *>(d_velocity), g.dimz,
+                             static_cast<const float *>(d_wavelet), nullptr));
+    RTM_TRY(dispatch_adjoint(&P, static_cast<const float *>(d_seismogram)));
+    RTM_TRY(image_to(&P, 0, d_image, 0, 0));
+    RTM_TRY(image_to(&P, 1, d_self_image, 0, 0));
+    return check_status(&P);
+}
