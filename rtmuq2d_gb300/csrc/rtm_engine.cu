@@ -95,7 +95,7 @@ static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 static int default_tile_x(const rtm_params &p)
 {
     (void)p;
-    return 32;
+    return 16;
 }
 
 static Geom make_geom(const rtm_params &p)
@@ -107,8 +107,11 @@ static Geom make_geom(const rtm_params &p)
     g.dimx = g.thl + g.nx + g.thr;
     g.dimz = g.thu + g.nz + g.thd;
     g.pitch = round_up(g.dimz, 32);
-    g.st = round_up(g.thu, 4);
-    g.sb = round_up(g.thd, 4);
+    // top/bottom strip arrays: z-aligned rows with 4 spare cells so that a quad's
+    // 12-value line (-4..+7) never leaves its row
+    g.st = round_up(g.thu, 4) + 4;
+    g.zb0 = (g.dimz - g.thd) & ~3;
+    g.sb = round_up(g.dimz - g.zb0, 4) + 4;
     g.xs = p.shot_x + g.thl;
     g.zs = p.shot_z + g.thu;
     g.zrec = g.thu + p.rec_depth;
@@ -119,8 +122,21 @@ static Geom make_geom(const rtm_params &p)
     g.ring_cells = 8 * g.ring_w + 8 * g.ring_h;
     g.nt = p.nt; g.nwav = p.n_wavelet; g.slices = p.time_slices; g.nrec = p.rec_count;
     g.tx = p.tile_x > 0 ? p.tile_x : default_tile_x(p);
+    if (p.compute == RTM_COMPUTE_FP64 && g.tx > 16) g.tx = 16;   // FP64 stages must fit in smem
     g.tiles_x = (g.dimx + g.tx - 1) / g.tx;
-    g.tiles_z = (g.dimz + TZ - 1) / TZ;
+    // z-tile 0 holds the top CPML band (corrections, ring) and, when they sit just below
+    // it, the receiver row and the shot, so that every other top tile is plain interior
+    {
+        int top = g.thu - 4;
+        if (g.zrec < g.thu + 16) top = std::max(top, g.zrec + 1);
+        if (g.zs < g.thu + 16) top = std::max(top, g.zs + 1);
+        g.ztop = std::min(TZ, std::max(4, round_up(top, 4)));
+        if (g.ztop >= g.dimz) g.ztop = std::min(TZ, round_up(g.dimz, 4));
+    }
+    g.tiles_z = g.dimz <= g.ztop ? 1 : 1 + (g.dimz - g.ztop + TZ - 1) / TZ;
+    g.tiles = g.tiles_x * g.tiles_z;
+    g.nxl = std::min(g.tiles_x, (g.thl - 4 + g.tx - 1) / g.tx);
+    g.xr0 = std::max(g.nxl, std::min(g.tiles_x, (g.dimx - g.thr + 4) / g.tx));
     return g;
 }
 
@@ -181,6 +197,47 @@ struct Layout {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Packed damping profiles, every array starting on a 16-byte boundary (see ProfLayout).
+static ProfLayout prof_layout(const Geom &g)
+{
+    ProfLayout pl;
+    const int len[8] = {g.thl, g.thl, g.thr, g.thr, g.st, g.st, g.sb, g.sb};
+    int off = 0;
+    for (int i = 0; i < 8; ++i) { pl.off[i] = off; off += round_up(len[i], 4); }
+    pl.total = off;
+    return pl;
+}
+
+// Packs reference-layout profiles (attenuation_profile_cpml's eight arrays) into `out`
+// (prof_layout(g).total floats): the bottom arrays move from index z-(dimZ-th_down) to
+// z - zb0; padding is zero.
+static void pack_profiles(const Geom &g, const float *a_l, const float *b_l, const float *a_r,
+                          const float *b_r, const float *a_t, const float *b_t, const float *a_b,
+                          const float *b_b, float *out)
+{
+    const ProfLayout pl = prof_layout(g);
+    memset(out, 0, sizeof(float) * (size_t)pl.total);
+    memcpy(out + pl.off[0], a_l, sizeof(float) * g.thl);
+    memcpy(out + pl.off[1], b_l, sizeof(float) * g.thl);
+    memcpy(out + pl.off[2], a_r, sizeof(float) * g.thr);
+    memcpy(out + pl.off[3], b_r, sizeof(float) * g.thr);
+    memcpy(out + pl.off[4], a_t, sizeof(float) * g.thu);
+    memcpy(out + pl.off[5], b_t, sizeof(float) * g.thu);
+    const int shift = (g.dimz - g.thd) - g.zb0;
+    memcpy(out + pl.off[6] + shift, a_b, sizeof(float) * g.thd);
+    memcpy(out + pl.off[7] + shift, b_b, sizeof(float) * g.thd);
+}
+
+// The reference's profiles for *p, packed.
+static void make_profiles(const rtm_params &p, const Geom &g, float *out)
+{
+    std::vector<float> ref(2 * (size_t)(g.thl + g.thr + g.thu + g.thd));
+    float *a_l = ref.data(), *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
+    float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
+    rtm_attenuation_profile_cpml(&p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
+    pack_profiles(g, a_l, b_l, a_r, b_r, a_t, b_t, a_b, b_b, out);
+}
+
 static Layout make_layout(const rtm_params &p, const Geom &g)
 {
     Layout L;
@@ -199,7 +256,7 @@ static Layout make_layout(const rtm_params &p, const Geom &g)
     L.psi[0] = take(n_l * es); L.psi[1] = take(n_r * es); L.psi[2] = take(n_t * es); L.psi[3] = take(n_b * es);
     L.xi[0] = take(n_l * es); L.xi[1] = take(n_r * es); L.xi[2] = take(n_t * es); L.xi[3] = take(n_b * es);
     L.strip_bytes = off - L.strips;
-    L.prof = take(sizeof(float) * 2 * (size_t)(g.thl + g.thr + g.thu + g.thd));
+    L.prof = take(sizeof(float) * (size_t)prof_layout(g).total);
     L.rec = take(sizeof(int) * 3 * (size_t)g.dimx);
     L.wav = take(sizeof(float) * (size_t)std::max(p.n_wavelet, 1));
     L.seis_t = take(sizeof(float) * (size_t)std::max(1, p.rec_count) * p.nt);
@@ -235,7 +292,9 @@ struct rtm_plan {
     unsigned char *base = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    CUtensorMap tm_u[2], tm_r[2];
+    CUtensorMap tm_u[2], tm_r[2];      // halo maps (box tx+8 x 136) of u[], r[]
+    CUtensorMap tm_up[2], tm_rp[2];    // plain maps (box tx x 128) of u[], r[]
+    CUtensorMap tm_c;                  // plain map of coef
     int cur_u = 0;        // u buffer holding u_nt after the forward pass
     int cur_r = 0;        // r buffer holding the last receiver field
     bool forward_done = false;
@@ -249,6 +308,13 @@ struct rtm_plan {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_launch[2];   // [forward, backward]
+    // CUDA graphs of the two time loops, captured on first use and replayed afterwards
+    bool use_graphs = true;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int graph_key[2] = {-1, -1};
+    long long graph_launches[2] = {0, 0};
+    int capture_pass = -1;       // pass being captured (0 forward, 1 backward), or -1
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> graph_events[2];
 
     template <typename T> T *at(size_t off) { return reinterpret_cast<T *>(base + off); }
 
@@ -265,6 +331,34 @@ struct rtm_plan {
 
 namespace rtm {
 
+// Plain 2-D map over a pitched field: box {TZ, tx} (no halo), zero fill out of range.
+static int make_plain_map(CUtensorMap *m, void *base, const Geom &g, size_t es)
+{
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return fail(RTM_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)g.pitch, (cuuint64_t)g.dimx};
+    cuuint64_t strides[1] = {(cuuint64_t)g.pitch * es};
+    cuuint32_t box[2] = {(cuuint32_t)TZ, (cuuint32_t)g.tx};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                     2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(RTM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return RTM_OK;
+}
+
+static int make_maps(rtm_plan *P)
+{
+    for (int i = 0; i < 2; ++i) {
+        RTM_TRY(make_field_map(&P->tm_u[i], P->base + P->L.u[i], P->g, P->es));
+        RTM_TRY(make_field_map(&P->tm_r[i], P->base + P->L.r[i], P->g, P->es));
+        RTM_TRY(make_plain_map(&P->tm_up[i], P->base + P->L.u[i], P->g, P->es));
+        RTM_TRY(make_plain_map(&P->tm_rp[i], P->base + P->L.r[i], P->g, P->es));
+    }
+    return make_plain_map(&P->tm_c, P->base + P->L.coef, P->g, P->es);
+}
+
 static int plan_alloc(const rtm_params &p, rtm_plan **out)
 {
     RTM_TRY(check_params(p));
@@ -278,18 +372,13 @@ static int plan_alloc(const rtm_params &p, rtm_plan **out)
         cudaGetLastError();
         return fail(RTM_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", P->L.total, cudaGetErrorString(e));
     }
-    for (int i = 0; i < 2; ++i) {
-        RTM_TRY(make_field_map(&P->tm_u[i], P->base + P->L.u[i], P->g, P->es));
-        RTM_TRY(make_field_map(&P->tm_r[i], P->base + P->L.r[i], P->g, P->es));
-    }
+    RTM_TRY(make_maps(P.get()));
     RTM_CUDA(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
     P->own_stream = true;
     // CPML profiles (host, reference arithmetic) and receiver maps
     const Geom &g = P->g;
-    std::vector<float> prof(2 * (size_t)(g.thl + g.thr + g.thu + g.thd));
-    float *a_l = prof.data(), *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
-    float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
-    rtm_attenuation_profile_cpml(&p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
+    std::vector<float> prof((size_t)prof_layout(g).total);
+    make_profiles(p, g, prof.data());
     P->h_prof = prof;
     std::vector<int> rec(3 * (size_t)g.dimx, 0);
     int *last = rec.data(), *first = last + g.dimx, *cnt = first + g.dimx;
@@ -317,6 +406,10 @@ static void plan_free(rtm_plan *P)
     if (P->base) cudaFree(P->base);
     if (P->h_pinned) cudaFreeHost(P->h_pinned);
     for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
+    for (int k = 0; k < 2; ++k) {
+        if (P->gexec[k]) cudaGraphExecDestroy(P->gexec[k]);
+        for (auto &pr : P->graph_events[k]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    }
     if (P->own_stream && P->stream) cudaStreamDestroy(P->stream);
     delete P;
 }
@@ -344,14 +437,14 @@ static void fill_common(rtm_plan *P, StepArgs<T> &a)
     a.h1 = (T)1.0f / dx;
     a.h2 = dx * dx;
     a.h3 = (T)1.0f / (dx * dx);
-    a.coef = P->at<T>(P->L.coef);
     a.psi_l = P->at<T>(P->L.psi[0]); a.psi_r = P->at<T>(P->L.psi[1]);
     a.psi_t = P->at<T>(P->L.psi[2]); a.psi_b = P->at<T>(P->L.psi[3]);
     a.xi_l = P->at<T>(P->L.xi[0]); a.xi_r = P->at<T>(P->L.xi[1]);
     a.xi_t = P->at<T>(P->L.xi[2]); a.xi_b = P->at<T>(P->L.xi[3]);
     const float *prof = P->at<float>(P->L.prof);
-    a.a_l = prof; a.b_l = prof + g.thl; a.a_r = a.b_l + g.thl; a.b_r = a.a_r + g.thr;
-    a.a_t = a.b_r + g.thr; a.b_t = a.a_t + g.thu; a.a_b = a.b_t + g.thu; a.b_b = a.a_b + g.thd;
+    const ProfLayout pl = prof_layout(g);
+    a.a_l = prof + pl.off[0]; a.b_l = prof + pl.off[1]; a.a_r = prof + pl.off[2]; a.b_r = prof + pl.off[3];
+    a.a_t = prof + pl.off[4]; a.b_t = prof + pl.off[5]; a.a_b = prof + pl.off[6]; a.b_b = prof + pl.off[7];
     const int *rec = P->at<int>(P->L.rec);
     a.rec_last = rec; a.rec_first = rec + g.dimx; a.rec_cnt = rec + 2 * g.dimx;
     a.store_prec = P->p.precision;
@@ -385,24 +478,84 @@ static float *scale_ptr(rtm_plan *P, int slot)
     return P->at<float>(P->L.scales) + (size_t)slot * P->L.n_scales_per_slot;
 }
 
+// Steps whose k_step launch is bracketed by profiling events (no programmatic overlap
+// across an event record).
+static bool sampled(const rtm_plan *P, int step)
+{
+    return P->prof_every > 0 && step % P->prof_every == 0;
+}
+
 // k_step launch, bracketed by CUDA events on sampled steps when profiling is on.
 template <typename T>
-static int timed_step(rtm_plan *P, int backward, int step, const CUtensorMap *tm_u,
-                      const CUtensorMap *tm_s, const StepArgs<T> &a)
+static int timed_step(rtm_plan *P, int backward, int step, const StepMaps &maps,
+                      const StepArgs<T> &a)
 {
-    const bool sample = P->prof_every > 0 && step % P->prof_every == 0;
+    const bool sample = sampled(P, step);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (sample) {
-        e0 = P->next_event();
-        e1 = P->next_event();
+        if (P->capture_pass >= 0) {      // events owned by the graph being captured
+            RTM_CUDA(cudaEventCreate(&e0));
+            RTM_CUDA(cudaEventCreate(&e1));
+        } else {
+            e0 = P->next_event();
+            e1 = P->next_event();
+        }
         if (!e0 || !e1) return fail(RTM_ERR_CUDA, "event pool");
-        RTM_CUDA(cudaEventRecord(e0, P->stream));
+        // inside a capture, an external event-record node keeps the event timeable
+        RTM_CUDA(cudaEventRecordWithFlags(e0, P->stream,
+                                          P->capture_pass >= 0 ? cudaEventRecordExternal : 0));
     }
-    RTM_CUDA(launch_step<T>(backward, tm_u, tm_s, a, P->stream));
+    const int grid = step_grid<T>(backward, P->g);
+    if (grid < 1) return fail(RTM_ERR_CUDA, "step kernel cannot be configured (tile_x %d)", P->g.tx);
+    // programmatic dependent launch: the step kernel overlaps the psi kernel before it
+    RTM_CUDA(launch_step<T>(backward, maps, a, grid, sample ? 0 : 1, P->stream));
     if (sample) {
-        RTM_CUDA(cudaEventRecord(e1, P->stream));
-        P->prof_launch[backward ? 1 : 0].push_back({e0, e1});
+        RTM_CUDA(cudaEventRecordWithFlags(e1, P->stream,
+                                          P->capture_pass >= 0 ? cudaEventRecordExternal : 0));
+        if (P->capture_pass >= 0) P->graph_events[P->capture_pass].push_back({e0, e1});
+        else P->prof_launch[backward ? 1 : 0].push_back({e0, e1});
     }
+    return RTM_OK;
+}
+
+// Issues one pass's time loop (`issue` launches it on P->stream) directly, or through a
+// CUDA graph captured on first use and replayed afterwards.  The kernels' arguments only
+// name plan-owned buffers, so one capture serves every later migration of the plan.
+template <typename F>
+static int run_loop(rtm_plan *P, int which, bool graphable, F issue)
+{
+    if (!graphable || !P->use_graphs) return issue();
+    const int key = P->prof_every;
+    if (!P->gexec[which] || P->graph_key[which] != key) {
+        if (P->gexec[which]) cudaGraphExecDestroy(P->gexec[which]);
+        P->gexec[which] = nullptr;
+        for (auto &pr : P->graph_events[which]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        P->graph_events[which].clear();
+        const long long before = P->launches;
+        RTM_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
+        P->capture_pass = which;
+        const int st = issue();
+        P->capture_pass = -1;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(P->stream, &graph);
+        if (st != RTM_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(RTM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+        const cudaError_t ei = cudaGraphInstantiate(&P->gexec[which], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            P->gexec[which] = nullptr;
+            return fail(RTM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        }
+        P->graph_launches[which] = P->launches - before;
+        P->launches = before;
+        P->graph_key[which] = key;
+    }
+    RTM_CUDA(cudaGraphLaunch(P->gexec[which], P->stream));
+    P->launches += P->graph_launches[which];
+    for (auto &pr : P->graph_events[which]) P->prof_launch[which].push_back(pr);
     return RTM_OK;
 }
 
@@ -426,31 +579,43 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
     PsiArgs<T> q;
     fill_psi<T>(P, a, q);
     const bool ring = P->p.storage == RTM_STORE_RING;
-    int c = 0;
-    for (int t = 0; t < g.nt; ++t) {
-        q.u = u[c];
-        RTM_CUDA(launch_psi<T>(q, s));
-        a.u_next = u[1 - c];
-        a.t = t;
-        int f = 0;
-        if (t < g.nwav) f |= F_SRC;
-        if (d_seis_out && g.nrec > 0) f |= F_RECORD;
-        a.store = nullptr;
-        a.store_scale = nullptr;
-        if (ring) {
-            f |= F_RING_SAVE;
-            a.store = slot_ptr(P, t + 1);
-            a.store_scale = scale_ptr(P, t + 1);
-        } else if (t % g.slices == 0) {
-            f |= F_SNAP_SAVE;
-            a.store = slot_ptr(P, t / g.slices);
-            a.store_scale = scale_ptr(P, t / g.slices);
+    (void)step_grid<T>(0, g);            // configure the kernels before any capture
+    auto loop = [&]() -> int {
+        int c = 0;
+        StepMaps maps;
+        for (int t = 0; t < g.nt; ++t) {
+            q.u = u[c];
+            RTM_CUDA(launch_psi<T>(q, t > 0 && !sampled(P, t - 1), s));
+            a.u_next = u[1 - c];
+            a.t = t;
+            int f = 0;
+            if (t < g.nwav) f |= F_SRC;
+            if (d_seis_out && g.nrec > 0) f |= F_RECORD;
+            a.store = nullptr;
+            a.store_scale = nullptr;
+            if (ring) {
+                f |= F_RING_SAVE;
+                a.store = slot_ptr(P, t + 1);
+                a.store_scale = scale_ptr(P, t + 1);
+            } else if (t % g.slices == 0) {
+                f |= F_SNAP_SAVE;
+                a.store = slot_ptr(P, t / g.slices);
+                a.store_scale = scale_ptr(P, t / g.slices);
+            }
+            a.flags = f;
+            maps.cur = P->tm_u[c];
+            maps.prev = P->tm_up[1 - c];
+            maps.coef = P->tm_c;
+            maps.scur = P->tm_u[c];
+            maps.sprev = P->tm_up[1 - c];
+            RTM_TRY(timed_step<T>(P, 0, t, maps, a));
+            P->launches += 2;
+            c ^= 1;
         }
-        a.flags = f;
-        RTM_TRY(timed_step<T>(P, 0, t, &P->tm_u[c], &P->tm_u[c], a));
-        P->launches += 2;
-        c ^= 1;
-    }
+        return RTM_OK;
+    };
+    RTM_TRY(run_loop(P, 0, d_seis_out == nullptr, loop));
+    const int c = g.nt & 1;             // u buffer holding u_nt
     P->cur_u = c;
     P->forward_done = true;
     P->image_valid = false;
@@ -495,52 +660,64 @@ static int run_adjoint(rtm_plan *P, const float *d_seis)
     fill_psi<T>(P, a, q);
     const bool ring = P->p.storage == RTM_STORE_RING;
     const int ua = P->cur_u, ub = 1 - P->cur_u;   // u_nt, u_{nt-1}
-    int sc = ub, sp = ua;                          // reconstruction: current / previous
-    int c = 0;
-    int ctrl = g.nt / g.slices - 1;                // backward_modeling.c:267
-    for (int time = 0; time < g.nt; ++time) {
-        const int tau = g.nt - time - 1;
-        int f = F_OVERWRITE;
-        a.seis_row = seis_t + (size_t)tau * std::max(g.nrec, 1);
-        if (g.nrec == 0) f &= ~F_OVERWRITE;
-        a.t = time;
-        a.store = nullptr;
-        a.store_scale = nullptr;
-        a.s_next = nullptr;
-        a.s_snap = nullptr;
-        a.s_fixed = nullptr;
-        const bool recon = ring && time >= 2;
-        if (recon) {
-            f |= F_RECON;
-            if (tau + 2 < g.nwav) f |= F_RECON_SRC;
-            a.s_next = u[sp];
-            a.store = slot_ptr(P, tau + 1);
-            a.store_scale = scale_ptr(P, tau + 1);
-        }
-        if (tau % g.slices == 0) {
-            if (ctrl >= 0) {
-                f |= F_IMAGE;
-                if (!ring) {
-                    f |= F_IMAGE_SNAP;
-                    a.s_snap = reinterpret_cast<const T *>(slot_ptr(P, ctrl));
-                    a.store = slot_ptr(P, ctrl);
-                    a.store_scale = scale_ptr(P, ctrl);
-                } else if (!recon) {
-                    f |= F_IMAGE_FIXED;
-                    a.s_fixed = time == 0 ? u[ua] : u[ub];
-                }
+    (void)step_grid<T>(1, g);            // configure the kernels before any capture
+    auto loop = [&]() -> int {
+        int sc = ub, sp = ua;                          // reconstruction: current / previous
+        int c = 0;
+        int ctrl = g.nt / g.slices - 1;                // backward_modeling.c:267
+        for (int time = 0; time < g.nt; ++time) {
+            const int tau = g.nt - time - 1;
+            int f = F_OVERWRITE;
+            a.seis_row = seis_t + (size_t)tau * std::max(g.nrec, 1);
+            if (g.nrec == 0) f &= ~F_OVERWRITE;
+            a.t = time;
+            a.store = nullptr;
+            a.store_scale = nullptr;
+            a.s_next = nullptr;
+            a.s_snap = nullptr;
+            a.s_fixed = nullptr;
+            const bool recon = ring && time >= 2;
+            if (recon) {
+                f |= F_RECON;
+                if (tau + 2 < g.nwav) f |= F_RECON_SRC;
+                a.s_next = u[sp];
+                a.store = slot_ptr(P, tau + 1);
+                a.store_scale = scale_ptr(P, tau + 1);
             }
-            ctrl--;
+            if (tau % g.slices == 0) {
+                if (ctrl >= 0) {
+                    f |= F_IMAGE;
+                    if (!ring) {
+                        f |= F_IMAGE_SNAP;
+                        a.s_snap = reinterpret_cast<const T *>(slot_ptr(P, ctrl));
+                        a.store = slot_ptr(P, ctrl);
+                        a.store_scale = scale_ptr(P, ctrl);
+                    } else if (!recon) {
+                        f |= F_IMAGE_FIXED;
+                        a.s_fixed = time == 0 ? u[ua] : u[ub];
+                    }
+                }
+                ctrl--;
+            }
+            a.flags = f;
+            q.u = r[c];
+            RTM_CUDA(launch_psi<T>(q, time > 0 && !sampled(P, time - 1), s));
+            a.u_next = r[1 - c];
+            StepMaps maps;
+            maps.cur = P->tm_r[c];
+            maps.prev = P->tm_rp[1 - c];
+            maps.coef = P->tm_c;
+            maps.scur = P->tm_u[sc];
+            maps.sprev = P->tm_up[sp];
+            RTM_TRY(timed_step<T>(P, 1, time, maps, a));
+            P->launches += 2;
+            c ^= 1;
+            if (recon) std::swap(sc, sp);
         }
-        a.flags = f;
-        q.u = r[c];
-        RTM_CUDA(launch_psi<T>(q, s));
-        a.u_next = r[1 - c];
-        RTM_TRY(timed_step<T>(P, 1, time, &P->tm_r[c], &P->tm_u[sc], a));
-        P->launches += 2;
-        c ^= 1;
-        if (recon) std::swap(sc, sp);
-    }
+        return RTM_OK;
+    };
+    RTM_TRY(run_loop(P, 1, true, loop));
+    const int c = g.nt & 1;             // r buffer holding the last receiver field
     P->cur_r = c;
     P->forward_done = false;   // the stored source wavefield has been consumed
     P->image_valid = true;
@@ -964,15 +1141,18 @@ static int field_to_host(rtm_plan *P, float *dst, const float *src)
 static int strips_io(rtm_plan *P, int to_device, float *const host[8])
 {
     const Geom &g = P->g;
-    struct { size_t off; int rows, host_w, dev_w; } s[8] = {
-        {P->L.psi[0], g.thl, g.dimz, g.pitch}, {P->L.psi[1], g.thr, g.dimz, g.pitch},
-        {P->L.psi[2], g.dimx, g.thu, g.st},    {P->L.psi[3], g.dimx, g.thd, g.sb},
-        {P->L.xi[0], g.thl, g.dimz, g.pitch},  {P->L.xi[1], g.thr, g.dimz, g.pitch},
-        {P->L.xi[2], g.dimx, g.thu, g.st},     {P->L.xi[3], g.dimx, g.thd, g.sb}};
+    // the bottom strip's reference rows start at z = dimZ - th_down, the device rows at zb0
+    const size_t bsh = (size_t)((g.dimz - g.thd) - g.zb0);
+    struct { size_t off; int rows, host_w, dev_w; size_t shift; } s[8] = {
+        {P->L.psi[0], g.thl, g.dimz, g.pitch, 0}, {P->L.psi[1], g.thr, g.dimz, g.pitch, 0},
+        {P->L.psi[2], g.dimx, g.thu, g.st, 0},    {P->L.psi[3], g.dimx, g.thd, g.sb, bsh},
+        {P->L.xi[0], g.thl, g.dimz, g.pitch, 0},  {P->L.xi[1], g.thr, g.dimz, g.pitch, 0},
+        {P->L.xi[2], g.dimx, g.thu, g.st, 0},     {P->L.xi[3], g.dimx, g.thd, g.sb, bsh}};
     for (int i = 0; i < 8; ++i) {
-        void *dev = P->base + s[i].off;
+        unsigned char *row0 = P->base + s[i].off;
+        float *dev = reinterpret_cast<float *>(row0) + s[i].shift;
         if (to_device) {
-            RTM_CUDA(cudaMemsetAsync(dev, 0, (size_t)s[i].rows * s[i].dev_w * sizeof(float), P->stream));
+            RTM_CUDA(cudaMemsetAsync(row0, 0, (size_t)s[i].rows * s[i].dev_w * sizeof(float), P->stream));
             RTM_CUDA(cudaMemcpy2DAsync(dev, s[i].dev_w * sizeof(float), host[i], s[i].host_w * sizeof(float),
                                        s[i].host_w * sizeof(float), s[i].rows, cudaMemcpyHostToDevice, P->stream));
         } else {
@@ -994,10 +1174,16 @@ static int one_step(rtm_plan *P, int flags, bool with_psi)
         PsiArgs<float> q;
         fill_psi<float>(P, a, q);
         q.u = P->at<float>(P->L.u[0]);
-        RTM_CUDA(launch_psi<float>(q, P->stream));
+        RTM_CUDA(launch_psi<float>(q, 0, P->stream));
         P->launches++;
     }
-    RTM_CUDA(launch_step<float>(0, &P->tm_u[0], &P->tm_u[0], a, P->stream));
+    StepMaps maps;
+    maps.cur = P->tm_u[0];
+    maps.prev = P->tm_up[1];
+    maps.coef = P->tm_c;
+    maps.scur = P->tm_u[0];
+    maps.sprev = P->tm_up[1];
+    RTM_CUDA(launch_step<float>(0, maps, a, step_grid<float>(0, P->g), 0, P->stream));
     P->launches++;
     return check_status(P);
 }
@@ -1040,12 +1226,7 @@ int rtm_aiso_attenuation_cpml(const rtm_params *p, const float *wave1, float *wa
     if (st == RTM_OK) st = strips_io(P, 1, strips);
     // caller-supplied profiles for this call; the plan's own are restored afterwards
     std::vector<float> prof(P->h_prof.size());
-    {
-        float *d = prof.data();
-        const float *src[8] = {a_left, b_left, a_right, b_right, a_top, b_top, a_bottom, b_bottom};
-        const int n[8] = {g.thl, g.thl, g.thr, g.thr, g.thu, g.thu, g.thd, g.thd};
-        for (int i = 0; i < 8; ++i) { memcpy(d, src[i], n[i] * sizeof(float)); d += n[i]; }
-    }
+    pack_profiles(g, a_left, b_left, a_right, b_right, a_top, b_top, a_bottom, b_bottom, prof.data());
     if (st == RTM_OK && cudaMemcpy(P->base + P->L.prof, prof.data(), prof.size() * sizeof(float),
                                    cudaMemcpyHostToDevice) != cudaSuccess)
         st = fail(RTM_ERR_CUDA, "profile upload");
@@ -1203,18 +1384,17 @@ extern "C" int rtm_migrate_shot_static(const rtm_params *p, const void *d_veloci
     P.base = static_cast<unsigned char *>(base);
     P.stream = static_cast<cudaStream_t>(stream);
     P.own_stream = false;
-    for (int i = 0; i < 2; ++i) {
-        RTM_TRY(make_field_map(&P.tm_u[i], P.base + L.u[i], g, P.es));
-        RTM_TRY(make_field_map(&P.tm_r[i], P.base + L.r[i], g, P.es));
-    }
+    P.use_graphs = false;                         // nothing outlives the call
+    RTM_TRY(make_maps(&P));
     // what the previous call left in the array: status word and receiver maps are rebuilt;
     // fields, strips and accumulators are zeroed by the forward / adjoint drivers
     RTM_CUDA(cudaMemsetAsync(P.base + L.status, 0, 256, P.stream));
-    float prof[8 * RTM_STATIC_MAX_THICK];
-    float *a_l = prof, *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
+    float ref[8 * RTM_STATIC_MAX_THICK], prof[8 * (RTM_STATIC_MAX_THICK + 16)];
+    float *a_l = ref, *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
     float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
     rtm_attenuation_profile_cpml(p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
-    RTM_CUDA(cudaMemcpyAsync(P.base + L.prof, prof, sizeof(float) * 2 * (size_t)(g.thl + g.thr + g.thu + g.thd),
+    pack_profiles(g, a_l, b_l, a_r, b_r, a_t, b_t, a_b, b_b, prof);
+    RTM_CUDA(cudaMemcpyAsync(P.base + L.prof, prof, sizeof(float) * (size_t)prof_layout(g).total,
                              cudaMemcpyHostToDevice, P.stream));
     int *rec = P.at<int>(L.rec);
     k_rec_maps<<<(g.dimx + 127) / 128, 128, 0, P.stream>>>(g, p->rec_first, p->rec_spacing, p->rec_count,

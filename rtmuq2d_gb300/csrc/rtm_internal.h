@@ -1,5 +1,5 @@
-// rtm_internal.h -- types shared by the sm_103a kernels (rtm_kernels.cu) and the host
-// engine (rtm_engine.cu).  Not part of the public C ABI.
+// rtm_internal.h -- types shared by the sm_103a kernels (rtm_kernels.cu, rtm_step.cuh) and
+// the host engine (rtm_engine.cu).  Not part of the public C ABI.
 #pragma once
 
 #include <cuda.h>
@@ -9,13 +9,14 @@
 namespace rtm {
 
 // ---- tile shape of the fused step kernel ------------------------------------------------
-// A CTA owns TX x TZ cells: lanes run along z (4 consecutive cells each, one 16-byte
-// vector for fp32), warps along x (RX columns per thread).  The current wavefield tile is
-// brought into shared memory by one TMA 2-D load with a 4-cell halo on every side.
+// A tile is TX x TZ cells: lanes run along z (4 consecutive cells each, one 16-byte vector
+// for fp32), warps along x (2 columns per thread).  The current-field tile is staged in
+// shared memory by a TMA 2-D copy with a 4-cell halo on every side; u_prev and coef tiles
+// by TMA copies without halo.
 constexpr int TZ = 128;               // z cells per tile  (32 lanes x 4)
 constexpr int HALO = 4;               // half stencil width (8th order)
-constexpr int SZ = TZ + 2 * HALO;     // shared-memory row length (z)
-constexpr int kMaxWarps = 8;
+constexpr int SZ = TZ + 2 * HALO;     // shared-memory row length of a halo tile (z)
+constexpr int RXC = 2;                // x columns per thread
 
 // Step flags (bit set in StepArgs::flags)
 enum : int {
@@ -31,6 +32,7 @@ enum : int {
     F_IMAGE_FIXED = 1 << 9,  // ...with S read from a resident buffer (first two steps)
     F_NO_STENCIL = 1 << 10,  // keep u_next as given (CPML-only drop-in step)
     F_NO_CPML = 1 << 11,     // skip the CPML corrections (stencil-only drop-in step)
+    F_PSI_READY = 1 << 12,   // psi needs no wait on a preceding k_psi (no PDL edge)
 };
 
 // Device-side error bits (StepArgs::status)
@@ -41,7 +43,9 @@ enum : unsigned {
 struct Geom {
     int nx, nz, thl, thr, thu, thd;
     int dimx, dimz, pitch;      // padded grid; pitch = z stride of every field (elements)
-    int st, sb;                 // z stride of the top / bottom CPML strip arrays
+    int st;                     // z stride of the top strip arrays (>= round4(thu) + 4)
+    int zb0;                    // first z of the bottom strip arrays (4-aligned, <= dimz-thd)
+    int sb;                     // z stride of the bottom strip arrays (>= round4(dimz-zb0) + 4)
     int xs, zs;                 // shot cell (padded coordinates)
     int zrec;                   // receiver row (padded)
     int rx0, rx1, rz0, rz1;     // reconstruction region [rx0,rx1) x [rz0,rz1)
@@ -49,14 +53,60 @@ struct Geom {
     int ring_cells;             // 8*ring_w + 8*ring_h
     int nt, nwav, slices, nrec;
     int tx;                     // x columns per tile
-    int tiles_x, tiles_z;
+    int ztop;                   // height of z-tile 0 (4-aligned, <= TZ): the top CPML band;
+                                // z-tile k >= 1 starts at ztop + (k-1)*TZ
+    int tiles_x, tiles_z, tiles;
+    int nxl, xr0;               // left CPML x-tiles [0,nxl), right ones [xr0,tiles_x)
+};
+
+// Scheduling order of the tiles of one step: the slow ones first -- the top and bottom
+// z-tiles (CPML strips, ring bands, receiver row), then the left/right CPML x-tiles of the
+// other z-tiles, then the plain interior.  x-tiles [0, nxl) and [xr0, tiles_x) are the
+// left/right CPML columns (nxl <= xr0).
+__host__ __device__ __forceinline__ void tile_coords(const Geom &g, int t, int &xt, int &zt)
+{
+    const int nzb = g.tiles_z > 1 ? 2 : 1;
+    const int n1 = g.tiles_x * nzb;
+    if (t < n1) {
+        xt = t / nzb;
+        zt = (t % nzb == 0) ? 0 : g.tiles_z - 1;
+        return;
+    }
+    t -= n1;
+    const int nzi = g.tiles_z - nzb;
+    const int nxb = g.nxl + (g.tiles_x - g.xr0);
+    if (t < nxb * nzi) {
+        const int xi = t / nzi;
+        xt = xi < g.nxl ? xi : g.xr0 + (xi - g.nxl);
+        zt = 1 + t % nzi;
+        return;
+    }
+    t -= nxb * nzi;
+    xt = g.nxl + t / nzi;
+    zt = 1 + t % nzi;
+}
+
+__host__ __device__ __forceinline__ int ztile_origin(const Geom &g, int zt)
+{
+    return zt == 0 ? 0 : g.ztop + (zt - 1) * TZ;
+}
+__host__ __device__ __forceinline__ int ztile_end(const Geom &g, int zt)
+{
+    return zt == 0 ? g.ztop : g.ztop + zt * TZ;
+}
+
+// Offsets (floats) of the eight damping profiles in the packed, 16-byte aligned profile
+// array: a_l b_l a_r b_r (by column), a_t b_t (by z, length st), a_b b_b (by z - zb0,
+// length sb).
+struct ProfLayout {
+    int off[8];
+    int total;
 };
 
 template <typename T>
 struct StepArgs {
     Geom g;
     T h1, h2, h3;               // 1/dx, dx^2, 1/dx^2 (absorbingBoundaryCondition.c:159-161)
-    const T *coef;
     T *u_next;                  // in: u_prev, out: u_next (in place, like the reference)
     const T *psi_l, *psi_r, *psi_t, *psi_b;
     T *xi_l, *xi_r, *xi_t, *xi_b;
@@ -79,6 +129,15 @@ struct StepArgs {
     unsigned *status;
 };
 
+// Tensor maps of one step: halo maps box {SZ, tx+8}, plain maps box {TZ, tx}.
+struct StepMaps {
+    CUtensorMap cur;            // current propagated field (halo)
+    CUtensorMap prev;           // previous propagated field = output buffer (plain)
+    CUtensorMap coef;           // (v dt/dx)^2 (plain)
+    CUtensorMap scur;           // backward reconstruction: current source field (halo)
+    CUtensorMap sprev;          // backward reconstruction: previous source field (plain)
+};
+
 template <typename T>
 struct PsiArgs {
     Geom g;
@@ -89,11 +148,15 @@ struct PsiArgs {
 };
 
 // ---- launchers (rtm_kernels.cu) --------------------------------------------------------
+// pdl: launch with programmatic stream serialization (overlaps the preceding kernel's tail)
 template <typename T>
-cudaError_t launch_step(int backward, const CUtensorMap *tm_u, const CUtensorMap *tm_s,
-                        const StepArgs<T> &a, cudaStream_t s);
+cudaError_t launch_step(int backward, const StepMaps &maps, const StepArgs<T> &a, int grid,
+                        int pdl, cudaStream_t s);
 template <typename T>
-cudaError_t launch_psi(const PsiArgs<T> &a, cudaStream_t s);
+cudaError_t launch_psi(const PsiArgs<T> &a, int pdl, cudaStream_t s);
+template <typename T>
+int step_grid(int backward, const Geom &g);      // persistent CTAs for one step
+size_t step_smem_bytes(int backward, int elem_size, int tx);
 template <typename T>
 cudaError_t launch_coef(const Geom &g, const float *vel, int vel_pitch, T *coef, float dx,
                         float dt, cudaStream_t s);
@@ -109,6 +172,5 @@ cudaError_t launch_laplacian(int nx, int nz, const float *in, float *out, cudaSt
 template <typename T>
 cudaError_t launch_xcorr(const Geom &g, const T *src, const T *rcv, double *img, double *slf,
                          cudaStream_t s);
-size_t step_smem_bytes(int backward, int elem_size, int tx);
 
 }  // namespace rtm

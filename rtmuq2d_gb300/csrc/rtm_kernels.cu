@@ -57,6 +57,11 @@ __device__ __forceinline__ void fence_barrier_init()
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -220,51 +225,82 @@ __device__ __forceinline__ float block_max(float v, float *red)
 
 #include "rtm_step.cuh"
 
-// ---- CPML psi update (runs before k_step) -------------------------------------------------
+// ---- CPML psi update (runs before k_step each step) ---------------------------------------
+// One thread per 4-cell quad of a strip: psi_n = b psi_{n-1} + a D1(u_n) / dx, the
+// reference's loops absorbingBoundaryCondition.c:171-189 (left), 219-235 (top), 265-281
+// (right), 312-328 (bottom).  With programmatic dependent launch it first waits for the
+// previous step kernel (whose output u_n it reads), then lets the next step kernel start.
 template <typename T>
-__global__ void __launch_bounds__(256) k_psi(const PsiArgs<T> a)
+__global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> a)
 {
+    griddep_wait();
+    griddep_launch();
     const Geom &g = a.g;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t P = (size_t)g.pitch;
-    switch (blockIdx.y) {
-    case 0: {   // left strip, x in [4, thl-4), z in [4, dimz-4)
-        const int w = g.dimz - 8;
-        if (idx >= (g.thl - 8) * w) return;
-        const int x = 4 + idx / w, z = 4 + idx % w;
-        const size_t at = (size_t)x * P + z;
-        a.psi_l[at] = (T)a.b_l[x] * a.psi_l[at] + (T)a.a_l[x] * d1<T>(a.u + at, (ptrdiff_t)P) * a.h1;
-        break;
+    const T h1 = a.h1;
+    if (blockIdx.y == 0 || blockIdx.y == 2) {        // left / right: x-derivative
+        const bool left = blockIdx.y == 0;
+        const int th = left ? g.thl : g.thr;
+        const int nq = (g.dimz - 8 + 3) / 4;
+        if (idx >= (th - 8) * nq) return;
+        const int li = 4 + idx / nq, zq = 4 + 4 * (idx % nq);
+        const int x = left ? li : g.dimx - g.thr + li;
+        T *psi = (left ? a.psi_l : a.psi_r) + (size_t)li * P + zq;
+        const T *u = a.u + (size_t)x * P + zq;
+        T m[4][4], p[4][4], ps[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            ld4(u - (ptrdiff_t)(4 - k) * (ptrdiff_t)P, m[k]);
+            ld4(u + (ptrdiff_t)(k + 1) * (ptrdiff_t)P, p[k]);
+        }
+        ld4(psi, ps);
+        const T ab = (T)(left ? a.a_l : a.a_r)[li], bb = (T)(left ? a.b_l : a.b_r)[li];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (zq + j < g.dimz - 4) ps[j] = bb * ps[j] + ab * dpsi_x<T>(m, p, j) * h1;
+        st4(psi, ps);
+        return;
     }
-    case 1: {   // top strip, x in [4, dimx-4), z in [4, thu-4)
-        const int w = g.thu - 8;
-        if (idx >= (g.dimx - 8) * w) return;
-        const int x = 4 + idx / w, z = 4 + idx % w;
-        const size_t ap = (size_t)x * g.st + z;
-        a.psi_t[ap] = (T)a.b_t[z] * a.psi_t[ap] + (T)a.a_t[z] * d1<T>(a.u + (size_t)x * P + z, 1) * a.h1;
-        break;
+    int x, zq, zlo, zhi;
+    T *psi;
+    const float *pa, *pb;
+    if (blockIdx.y == 1) {                           // top: z-derivative, z in [4, thu-4)
+        const int nq = (g.thu - 8 + 3) / 4;
+        if (idx >= (g.dimx - 8) * nq) return;
+        x = 4 + idx / nq;
+        zq = 4 + 4 * (idx % nq);
+        zlo = 4; zhi = g.thu - 4;
+        psi = a.psi_t + (size_t)x * g.st + zq;
+        pa = a.a_t + zq; pb = a.b_t + zq;
+    } else {                                          // bottom: z in [dimz-thd+4, dimz-4)
+        zlo = g.dimz - g.thd + 4; zhi = g.dimz - 4;
+        const int q0 = zlo & ~3;
+        const int nq = (zhi - q0 + 3) / 4;
+        if (idx >= (g.dimx - 8) * nq) return;
+        x = 4 + idx / nq;
+        zq = q0 + 4 * (idx % nq);
+        psi = a.psi_b + (size_t)x * g.sb + (zq - g.zb0);
+        pa = a.a_b + (zq - g.zb0); pb = a.b_b + (zq - g.zb0);
     }
-    case 2: {   // right strip, x in [dimx-thr+4, dimx-4)
-        const int w = g.dimz - 8;
-        if (idx >= (g.thr - 8) * w) return;
-        const int li = 4 + idx / w, z = 4 + idx % w;
-        const int x = g.dimx - g.thr + li;
-        const size_t ap = (size_t)li * P + z;
-        a.psi_r[ap] = (T)a.b_r[li] * a.psi_r[ap] +
-                      (T)a.a_r[li] * d1<T>(a.u + (size_t)x * P + z, (ptrdiff_t)P) * a.h1;
-        break;
+    const T *u = a.u + (size_t)x * P + zq;
+    T q[12], ps[4];
+    {
+        T a0[4], a1[4], a2[4];
+        ld4(u - 4, a0); ld4(u, a1); ld4(u + 4, a2);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { q[j] = a0[j]; q[4 + j] = a1[j]; q[8 + j] = a2[j]; }
     }
-    default: {  // bottom strip, z in [dimz-thd+4, dimz-4)
-        const int w = g.thd - 8;
-        if (idx >= (g.dimx - 8) * w) return;
-        const int x = 4 + idx / w, lz = 4 + idx % w;
-        const int z = g.dimz - g.thd + lz;
-        const size_t ap = (size_t)x * g.sb + lz;
-        a.psi_b[ap] = (T)a.b_b[lz] * a.psi_b[ap] +
-                      (T)a.a_b[lz] * d1<T>(a.u + (size_t)x * P + z, 1) * a.h1;
-        break;
+    ld4(psi, ps);
+    const float4 av = *reinterpret_cast<const float4 *>(pa);
+    const float4 bv = *reinterpret_cast<const float4 *>(pb);
+    const float aa[4] = {av.x, av.y, av.z, av.w}, bb[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = zq + j;
+        if (z >= zlo && z < zhi) ps[j] = (T)bb[j] * ps[j] + (T)aa[j] * dpsi_z<T>(q, j) * h1;
     }
-    }
+    st4(psi, ps);
 }
 
 // ---- set-up and layout kernels ------------------------------------------------------------
@@ -357,61 +393,131 @@ __global__ void k_xcorr(Geom g, const T *src, const T *rcv, double *img, double 
 }
 
 // ---- launchers ---------------------------------------------------------------------------
-size_t step_smem_bytes(int backward, int elem_size, int tx)
+static cudaLaunchAttribute pdl_attr()
 {
-    return (size_t)(tx + 2 * HALO) * SZ * elem_size * (backward ? 2 : 1);
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    return at;
 }
 
 template <typename T, int BWD, int WARPS>
-static cudaError_t launch_step_w(const CUtensorMap *tm_u, const CUtensorMap *tm_s,
-                                 const StepArgs<T> &a, cudaStream_t s)
+static cudaError_t configure_step()
 {
-    const size_t smem = step_smem_bytes(BWD, sizeof(T), StepCfg<T, WARPS>::TXC);
-    static bool configured = false;   // attribute set once per instantiation
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_step<T, BWD, WARPS>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
+    static cudaError_t state = cudaErrorNotReady;   // attribute set once per instantiation
+    if (state == cudaErrorNotReady) {
+        state = cudaFuncSetAttribute(k_step<T, BWD, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)StepCfg<T, WARPS, BWD>::SMEM);
+        // every per-step kernel asks for the same L1/shared split, so alternating kernels do
+        // not make the SMs drain and reconfigure the carveout at each launch
+        if (state == cudaSuccess)
+            state = cudaFuncSetAttribute(k_step<T, BWD, WARPS>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         cudaSharedmemCarveoutMaxShared);
     }
-    dim3 grid(a.g.tiles_x, a.g.tiles_z);
-    k_step<T, BWD, WARPS><<<grid, WARPS * 32, smem, s>>>(*tm_u, *tm_s, a);
-    return cudaGetLastError();
+    return state;
+}
+
+template <typename T, int BWD, int WARPS>
+static cudaError_t launch_step_w(const StepMaps &m, const StepArgs<T> &a, int grid, int pdl,
+                                 cudaStream_t s)
+{
+    cudaError_t e = configure_step<T, BWD, WARPS>();
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(WARPS * 32);
+    cfg.dynamicSmemBytes = StepCfg<T, WARPS, BWD>::SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute at = pdl_attr();
+    cfg.attrs = pdl ? &at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_step<T, BWD, WARPS>, m, a);
+}
+
+template <typename T, int BWD, int WARPS>
+static int grid_w(const Geom &g)
+{
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        if (configure_step<T, BWD, WARPS>() != cudaSuccess) return 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<T, BWD, WARPS>, WARPS * 32,
+                                                      StepCfg<T, WARPS, BWD>::SMEM);
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int full = per_sm * sms;
+    return g.tiles < full ? g.tiles : full;
 }
 
 template <typename T>
-cudaError_t launch_step(int backward, const CUtensorMap *tm_u, const CUtensorMap *tm_s,
-                        const StepArgs<T> &a, cudaStream_t s)
+int step_grid(int backward, const Geom &g)
 {
-    const int warps = a.g.tx / StepCfg<T, 4>::RXC;
+    const int warps = g.tx / RXC;
     if (backward) {
-        switch (warps) {
-        case 4: return launch_step_w<T, 1, 4>(tm_u, tm_s, a, s);
-        case 8: return launch_step_w<T, 1, 8>(tm_u, tm_s, a, s);
-        case 16: return launch_step_w<T, 1, 16>(tm_u, tm_s, a, s);
-        default: return cudaErrorInvalidValue;
-        }
+        if (warps == 4) return grid_w<T, 1, 4>(g);
+        if (warps == 8) return grid_w<T, 1, 8>(g);
+        if (warps == 16 && sizeof(T) == 4) return grid_w<T, 1, (sizeof(T) == 4 ? 16 : 8)>(g);
+        return 0;
     }
-    switch (warps) {
-    case 4: return launch_step_w<T, 0, 4>(tm_u, tm_s, a, s);
-    case 8: return launch_step_w<T, 0, 8>(tm_u, tm_s, a, s);
-    case 16: return launch_step_w<T, 0, 16>(tm_u, tm_s, a, s);
-    default: return cudaErrorInvalidValue;
-    }
+    if (warps == 4) return grid_w<T, 0, 4>(g);
+    if (warps == 8) return grid_w<T, 0, 8>(g);
+    if (warps == 16 && sizeof(T) == 4) return grid_w<T, 0, (sizeof(T) == 4 ? 16 : 8)>(g);
+    return 0;
+}
+
+size_t step_smem_bytes(int backward, int elem_size, int tx)
+{
+    const size_t ut = (size_t)(tx + 2 * HALO) * SZ, pt = (size_t)tx * TZ;
+    const size_t stage = backward ? 2 * ut + 3 * pt : ut + 2 * pt;
+    const size_t ns = (elem_size == 4 && !backward) ? 3 : 2;
+    return ns * stage * elem_size;
 }
 
 template <typename T>
-cudaError_t launch_psi(const PsiArgs<T> &a, cudaStream_t s)
+cudaError_t launch_step(int backward, const StepMaps &maps, const StepArgs<T> &a, int grid,
+                        int pdl, cudaStream_t s)
+{
+    const int warps = a.g.tx / RXC;
+    if (grid < 1) return cudaErrorInvalidConfiguration;
+    if (backward) {
+        if (warps == 4) return launch_step_w<T, 1, 4>(maps, a, grid, pdl, s);
+        if (warps == 8) return launch_step_w<T, 1, 8>(maps, a, grid, pdl, s);
+        if (warps == 16 && sizeof(T) == 4)
+            return launch_step_w<T, 1, (sizeof(T) == 4 ? 16 : 8)>(maps, a, grid, pdl, s);
+        return cudaErrorInvalidValue;
+    }
+    if (warps == 4) return launch_step_w<T, 0, 4>(maps, a, grid, pdl, s);
+    if (warps == 8) return launch_step_w<T, 0, 8>(maps, a, grid, pdl, s);
+    if (warps == 16 && sizeof(T) == 4)
+        return launch_step_w<T, 0, (sizeof(T) == 4 ? 16 : 8)>(maps, a, grid, pdl, s);
+    return cudaErrorInvalidValue;
+}
+
+template <typename T>
+cudaError_t launch_psi(const PsiArgs<T> &a, int pdl, cudaStream_t s)
 {
     const Geom &g = a.g;
-    int n = (g.thl - 8) * (g.dimz - 8);
-    n = n > (g.thr - 8) * (g.dimz - 8) ? n : (g.thr - 8) * (g.dimz - 8);
-    n = n > (g.thu - 8) * (g.dimx - 8) ? n : (g.thu - 8) * (g.dimx - 8);
-    n = n > (g.thd - 8) * (g.dimx - 8) ? n : (g.thd - 8) * (g.dimx - 8);
-    dim3 grid((n + 255) / 256, 4);
-    k_psi<T><<<grid, 256, 0, s>>>(a);
-    return cudaGetLastError();
+    const int nlr = (g.dimz - 8 + 3) / 4;
+    int n = (g.thl - 8) * nlr;
+    n = n > (g.thr - 8) * nlr ? n : (g.thr - 8) * nlr;
+    n = n > (g.dimx - 8) * ((g.thu - 8 + 3) / 4) ? n : (g.dimx - 8) * ((g.thu - 8 + 3) / 4);
+    const int q0 = (g.dimz - g.thd + 4) & ~3;
+    const int nb = (g.dimx - 8) * ((g.dimz - 4 - q0 + 3) / 4);
+    n = n > nb ? n : nb;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((n + 255) / 256, 4);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute at = pdl_attr();
+    cfg.attrs = pdl ? &at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    static cudaError_t carve = cudaFuncSetAttribute(k_psi<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                    cudaSharedmemCarveoutMaxShared);
+    if (carve != cudaSuccess) return carve;
+    return cudaLaunchKernelEx(&cfg, k_psi<T>, a);
 }
 
 template <typename T>
@@ -472,9 +578,10 @@ cudaError_t launch_xcorr(const Geom &g, const T *src, const T *rcv, double *img,
 }
 
 #define RTM_INSTANTIATE(T)                                                                      \
-    template cudaError_t launch_step<T>(int, const CUtensorMap *, const CUtensorMap *,         \
-                                        const StepArgs<T> &, cudaStream_t);                    \
-    template cudaError_t launch_psi<T>(const PsiArgs<T> &, cudaStream_t);                      \
+    template cudaError_t launch_step<T>(int, const StepMaps &, const StepArgs<T> &, int, int,  \
+                                        cudaStream_t);                                         \
+    template int step_grid<T>(int, const Geom &);                                              \
+    template cudaError_t launch_psi<T>(const PsiArgs<T> &, int, cudaStream_t);                 \
     template cudaError_t launch_coef<T>(const Geom &, const float *, int, T *, float, float,   \
                                         cudaStream_t);                                         \
     template cudaError_t launch_image_out<T>(const Geom &, const double *, T *, int,           \
