@@ -271,10 +271,15 @@ def run_gpu(args):
         plan.forward(d_vel, d_wav)
         plan.adjoint(d_seis, d_img, d_slf)
 
+    # Sampled kernel timing (every 16th step's k_step bracketed by CUDA events) is switched
+    # on before the warm-up, so the time-loop graphs are captured with those events outside
+    # the timed region; the timed migrations replay them.
+    plan.profile(16)
     torch.cuda.synchronize()
     for _ in range(args.warmup):
         migrate()
     torch.cuda.synchronize()
+    plan.profile_read()
 
     def barrier():
         if ws > 1:
@@ -284,7 +289,6 @@ def run_gpu(args):
 
     sampler = ClockSampler(local)
     launches0 = plan.launches
-    plan.profile(16)
     times = []
     barrier()
     with sampler:
@@ -360,7 +364,8 @@ def run_gpu(args):
                 "avg_launch_ms": bwd_avg_ms, "sampled_launches": prof["bwd_n"],
                 "fwd_kernel_avg_launch_ms": fwd_avg_ms,
                 "fwd_kernel_achieved_gbs": nbytes["k_step_fwd"] / (fwd_avg_ms * 1e-3) / 1e9,
-                "note": "working set of one 3500x800 grid (~45 MB/step) is L2-resident"}
+                "note": "fields stream from HBM every step (warm-cache ncu: 37 MB read per "
+                        "forward step, L2 hit rate 47%); traffic: cold-cache ncu reads"}
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
