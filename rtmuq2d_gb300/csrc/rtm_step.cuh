@@ -473,16 +473,20 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
                     ld4(a.s_fixed + (size_t)x * P + zq, s);
                 }
             }
+            // the receiver quad this thread stored above (reloaded rather than kept live
+            // through the reconstruction, which keeps the kernel at two CTAs per SM)
+            T rv[4];
+            ld4(a.u_next + (size_t)x * P + zq, rv);
             if (image_fast) {
                 const size_t o = (size_t)(x - g.thl) * P + zq;
-                image_quad<T>(a.img + o, a.slf + o, s, v[r]);
+                image_quad<T>(a.img + o, a.slf + o, s, rv);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int z = zq + j;
                     if (z < g.dimz && in_interior(g, x, z)) {
                         const size_t o = (size_t)(x - g.thl) * P + z;
-                        a.img[o] += (double)s[j] * (double)v[r][j];
+                        a.img[o] += (double)s[j] * (double)rv[j];
                         a.slf[o] += (double)s[j] * (double)s[j];
                     }
                 }
@@ -492,7 +496,7 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
 }
 
 template <typename T, int BWD, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8 && !BWD) ? 2 : 1)
+__global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2 : 1)
     k_step(const __grid_constant__ StepMaps m, const __grid_constant__ StepArgs<T> a)
 {
     using Cfg = StepCfg<T, WARPS, BWD>;
