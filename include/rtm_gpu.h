@@ -188,6 +188,34 @@ int rtm_plan_profile_read(rtm_plan *plan, double *fwd_ms, int *fwd_n, double *bw
 /* Frees the plans the host-buffer entry points keep for reuse. */
 void rtm_release_cached(void);
 
+/* ---- serving and batching ------------------------------------------------------------------
+ * Replaces the reference's MPI fan-out over simulations (SRC/mpi_rtm_iso2d.c:39-51: ranks
+ * run rtm_routine for disjoint simulation ranges, with no messages) by many migrations
+ * resident on one GPU.  A server admits submitted migrations (any grid, time axis, storage
+ * precision; FP32 compute) in arrival order while a member slot is free and their footprint
+ * fits the HBM budget, and advances every resident migration one time step per batched step
+ * -- one k_bpsi + one k_bstep launch over a (migration, tile) work list, replayed from a
+ * CUDA graph.  Finished migrations free their slots for the next admissions (continuous
+ * batching).  One thread drives a server. */
+typedef struct rtm_server rtm_server;
+
+/* hbm_budget_bytes <= 0: 80 % of the free device memory.  max_members <= 128. */
+int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per_launch,
+                      rtm_server **server);
+int rtm_server_destroy(rtm_server *server);
+/* Queues one migration; the host arrays are copied (velocity: padded dimX x dimZ,
+ * wavelet: n_wavelet, seismogram: rec_count x nt). */
+int rtm_server_submit(rtm_server *server, const rtm_params *p, const float *velocity,
+                      const float *wavelet, const float *seismogram, long long *request_id);
+/* Admits, runs steps_per_launch batched steps, harvests finished migrations. */
+int rtm_server_step(rtm_server *server, int *n_active, int *n_queued);
+/* One finished migration (RTM_ERR_BUSY if none): image and self image (nx x nz, each may be
+ * NULL), times[3] = submit, admission, completion (seconds, monotonic clock; may be NULL). */
+int rtm_server_poll(rtm_server *server, long long *request_id, float *image, float *self_image,
+                    double *times);
+int rtm_server_stats(const rtm_server *server, long long *cell_updates, double *gpu_ms,
+                     long long *launches, long long *bytes_in_use);
+
 /* ---- migration without device allocation -------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc: a host whose
  * device memory is owned by another allocator or held to a fixed budget, or a serving loop

@@ -137,6 +137,14 @@ def _declare(L):
         "rtm_plan_launch_count": (C.c_longlong, [vp]),
         "rtm_plan_bytes": (C.c_longlong, [vp]),
         "rtm_release_cached": (None, []),
+        "rtm_server_create": (C.c_int, [C.c_longlong, C.c_int, C.c_int, C.POINTER(vp)]),
+        "rtm_server_destroy": (C.c_int, [vp]),
+        "rtm_server_submit": (C.c_int, [vp, P, fp, fp, fp, C.POINTER(C.c_longlong)]),
+        "rtm_server_step": (C.c_int, [vp, ip, ip]),
+        "rtm_server_poll": (C.c_int, [vp, C.POINTER(C.c_longlong), fp, fp, C.POINTER(C.c_double)]),
+        "rtm_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "rtm_migrate_shot_static": (C.c_int, [P, vp, vp, vp, vp, vp, vp]),
         "rtm_plan_profile": (C.c_int, [vp, C.c_int]),
         "rtm_plan_profile_read": (C.c_int, [vp, C.POINTER(C.c_double), ip, C.POINTER(C.c_double), ip]),
     }
@@ -155,7 +163,9 @@ def exported_symbols():
             "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_plan_create",
             "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
             "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_launch_count",
-            "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read"]
+            "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
+            "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_step",
+            "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static"]
 
 
 def status_string(st: int) -> str:
@@ -335,3 +345,75 @@ class Plan:
     @property
     def nbytes(self) -> int:
         return int(lib().rtm_plan_bytes(self.handle))
+
+
+# ---- serving / batching -------------------------------------------------------------------
+class Server:
+    """Continuous-batching server of resident migrations (include/rtm_gpu.h, rtm_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_members: int = 64, steps_per_launch: int = 16):
+        h = C.c_void_p()
+        _check(lib().rtm_server_create(hbm_budget_bytes, max_members, steps_per_launch, C.byref(h)))
+        self.handle = h
+        self.params = {}
+
+    def close(self):
+        if self.handle:
+            lib().rtm_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, p: RtmParams, velocity, wavelet, seismogram) -> int:
+        rid = C.c_longlong()
+        q = p.replace()
+        _check(lib().rtm_server_submit(self.handle, C.byref(q), _fp(_f32(velocity)), _fp(_f32(wavelet)),
+                                       _fp(_f32(seismogram)), C.byref(rid)))
+        self.params[rid.value] = q
+        return rid.value
+
+    def step(self):
+        a, qd = C.c_int(), C.c_int()
+        _check(lib().rtm_server_step(self.handle, C.byref(a), C.byref(qd)))
+        return a.value, qd.value
+
+    def poll(self):
+        """(request_id, image, self_image, (t_submit, t_admit, t_done)) or None."""
+        if not self.params:
+            return None
+        # the finished request's size is unknown until polled: use the largest pending one
+        n = max(p.nx * p.nz for p in self.params.values())
+        img = np.zeros(n, np.float32)
+        slf = np.zeros(n, np.float32)
+        rid = C.c_longlong()
+        times = (C.c_double * 3)()
+        st = lib().rtm_server_poll(self.handle, C.byref(rid), _fp(img), _fp(slf), times)
+        if st == RTM_ERR_BUSY:
+            return None
+        _check(st)
+        p = self.params.pop(rid.value)
+        m = p.nx * p.nz
+        return (rid.value, img[:m].reshape(p.nx, p.nz).copy(), slf[:m].reshape(p.nx, p.nz).copy(),
+                tuple(times))
+
+    def stats(self) -> dict:
+        cu, ms, ln, by = C.c_longlong(), C.c_double(), C.c_longlong(), C.c_longlong()
+        _check(lib().rtm_server_stats(self.handle, C.byref(cu), C.byref(ms), C.byref(ln), C.byref(by)))
+        return {"cell_updates": cu.value, "gpu_ms": ms.value, "launches": ln.value, "bytes_in_use": by.value}
+
+    def run_all(self):
+        """Steps until every submitted migration has finished; returns {id: (img, self, times)}."""
+        out = {}
+        while True:
+            active, queued = self.step()
+            while True:
+                r = self.poll()
+                if r is None:
+                    break
+                out[r[0]] = r[1:]
+            if active == 0 and queued == 0 and not self.params:
+                return out

@@ -9,9 +9,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -1407,3 +1409,5 @@ extern "C" int rtm_migrate_shot_static(const rtm_params *p, const void *d_veloci
     RTM_TRY(image_to(&P, 1, d_self_image, 0, 0));
     return check_status(&P);
 }
+
+#include "rtm_serve.cuh"

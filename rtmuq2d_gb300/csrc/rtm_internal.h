@@ -32,7 +32,7 @@ enum : int {
     F_IMAGE_FIXED = 1 << 9,  // ...with S read from a resident buffer (first two steps)
     F_NO_STENCIL = 1 << 10,  // keep u_next as given (CPML-only drop-in step)
     F_NO_CPML = 1 << 11,     // skip the CPML corrections (stencil-only drop-in step)
-    F_PSI_READY = 1 << 12,   // psi needs no wait on a preceding k_psi (no PDL edge)
+    F_STRIPS_FRESH = 1 << 12,  // first step of a pass: psi/xi start from zero (batched members)
 };
 
 // Device-side error bits (StepArgs::status)
@@ -138,6 +138,35 @@ struct StepMaps {
     CUtensorMap sprev;          // backward reconstruction: previous source field (plain)
 };
 
+// One member of a batch (a resident migration): descriptor read by k_bpsi / k_bstep.
+template <typename T>
+struct BMember {                 // aligned like its leading tensor maps
+    CUtensorMap tm_u[2], tm_up[2], tm_r[2], tm_rp[2], tm_c;   // halo / plain maps
+    Geom g;
+    T h1, h2, h3;
+    T *u[2], *r[2];
+    T *psi[4], *xi[4];          // left, right, top, bottom
+    const float *prof[8];       // a_l b_l a_r b_r a_t b_t a_b b_b (packed, see ProfLayout)
+    const int *rec_last, *rec_first, *rec_cnt;
+    const float *wav, *seis_t;
+    double *img, *slf;
+    void *store;
+    size_t slot_elems;
+    float *scales;
+    int store_prec, storage;
+    unsigned *status;
+};
+
+constexpr int kMaxMembers = 128;   // members of one batch
+
+// Work lists of one batch: member i owns global tiles [tile_base[i], tile_base[i+1]) and
+// psi quads [psi_base[i], psi_base[i+1]).
+struct BatchIndex {
+    int nmem;
+    int tile_base[kMaxMembers + 1];
+    int psi_base[kMaxMembers + 1];
+};
+
 template <typename T>
 struct PsiArgs {
     Geom g;
@@ -146,6 +175,19 @@ struct PsiArgs {
     T *psi_l, *psi_r, *psi_t, *psi_b;
     const float *a_l, *b_l, *a_r, *b_r, *a_t, *b_t, *a_b, *b_b;
 };
+
+// ---- batched steps (rtm_batch.cuh) -------------------------------------------------------
+// state[m] = (pass, step): pass 0 idle, 1 forward, 2 backward, 3 finished.
+// done[0]: CTA counter of the step in flight (zero between launches); done[1]: error bits.
+template <typename T>
+cudaError_t launch_bpsi(const BatchIndex *ix, const BMember<T> *mem, const int2 *state, int grid,
+                        int pdl, cudaStream_t s);
+template <typename T>
+cudaError_t launch_bstep(const BatchIndex *ix, const BMember<T> *mem, int2 *state, unsigned *done,
+                         int grid, int pdl, cudaStream_t s);
+template <typename T>
+int bstep_grid();                                 // persistent CTAs of k_bstep
+void psi_counts_host(const Geom &g, int (&n)[4]);
 
 // ---- launchers (rtm_kernels.cu) --------------------------------------------------------
 // pdl: launch with programmatic stream serialization (overlaps the preceding kernel's tail)

@@ -225,54 +225,55 @@ __device__ __forceinline__ float block_max(float v, float *red)
 
 #include "rtm_step.cuh"
 
-// ---- CPML psi update (runs before k_step each step) ---------------------------------------
-// One thread per 4-cell quad of a strip: psi_n = b psi_{n-1} + a D1(u_n) / dx, the
-// reference's loops absorbingBoundaryCondition.c:171-189 (left), 219-235 (top), 265-281
-// (right), 312-328 (bottom).  With programmatic dependent launch it first waits for the
-// previous step kernel (whose output u_n it reads), then lets the next step kernel start.
+// ---- CPML psi update ----------------------------------------------------------------------
+// One 4-cell quad of a strip: psi_n = b psi_{n-1} + a D1(u_n) / dx, the reference's loops
+// absorbingBoundaryCondition.c:171-189 (left), 219-235 (top), 265-281 (right), 312-328
+// (bottom).  strip: 0 left, 1 top, 2 right, 3 bottom; idx: quad index within the strip;
+// psi: {left, right, top, bottom}; prof: packed a/b profiles; fresh: psi_{n-1} = 0.
 template <typename T>
-__global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> a)
+__device__ __forceinline__ void psi_quad(const Geom &g, T h1, const T *u0, T *const *psi,
+                                         const float *const *prof, int strip, int idx, bool fresh)
 {
-    griddep_wait();
-    griddep_launch();
-    const Geom &g = a.g;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t P = (size_t)g.pitch;
-    const T h1 = a.h1;
-    if (blockIdx.y == 0 || blockIdx.y == 2) {        // left / right: x-derivative
-        const bool left = blockIdx.y == 0;
+    if (strip == 0 || strip == 2) {                  // left / right: x-derivative
+        const bool left = strip == 0;
         const int th = left ? g.thl : g.thr;
         const int nq = (g.dimz - 8 + 3) / 4;
         if (idx >= (th - 8) * nq) return;
         const int li = 4 + idx / nq, zq = 4 + 4 * (idx % nq);
         const int x = left ? li : g.dimx - g.thr + li;
-        T *psi = (left ? a.psi_l : a.psi_r) + (size_t)li * P + zq;
-        const T *u = a.u + (size_t)x * P + zq;
+        T *ps4 = (left ? psi[0] : psi[1]) + (size_t)li * P + zq;
+        const T *u = u0 + (size_t)x * P + zq;
         T m[4][4], p[4][4], ps[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             ld4(u - (ptrdiff_t)(4 - k) * (ptrdiff_t)P, m[k]);
             ld4(u + (ptrdiff_t)(k + 1) * (ptrdiff_t)P, p[k]);
         }
-        ld4(psi, ps);
-        const T ab = (T)(left ? a.a_l : a.a_r)[li], bb = (T)(left ? a.b_l : a.b_r)[li];
+        if (fresh) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) ps[j] = (T)0;
+        } else {
+            ld4(ps4, ps);
+        }
+        const T ab = (T)(left ? prof[0] : prof[2])[li], bb = (T)(left ? prof[1] : prof[3])[li];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             if (zq + j < g.dimz - 4) ps[j] = bb * ps[j] + ab * dpsi_x<T>(m, p, j) * h1;
-        st4(psi, ps);
+        st4(ps4, ps);
         return;
     }
     int x, zq, zlo, zhi;
-    T *psi;
+    T *ps4;
     const float *pa, *pb;
-    if (blockIdx.y == 1) {                           // top: z-derivative, z in [4, thu-4)
+    if (strip == 1) {                                // top: z-derivative, z in [4, thu-4)
         const int nq = (g.thu - 8 + 3) / 4;
         if (idx >= (g.dimx - 8) * nq) return;
         x = 4 + idx / nq;
         zq = 4 + 4 * (idx % nq);
         zlo = 4; zhi = g.thu - 4;
-        psi = a.psi_t + (size_t)x * g.st + zq;
-        pa = a.a_t + zq; pb = a.b_t + zq;
+        ps4 = psi[2] + (size_t)x * g.st + zq;
+        pa = prof[4] + zq; pb = prof[5] + zq;
     } else {                                          // bottom: z in [dimz-thd+4, dimz-4)
         zlo = g.dimz - g.thd + 4; zhi = g.dimz - 4;
         const int q0 = zlo & ~3;
@@ -280,10 +281,10 @@ __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> 
         if (idx >= (g.dimx - 8) * nq) return;
         x = 4 + idx / nq;
         zq = q0 + 4 * (idx % nq);
-        psi = a.psi_b + (size_t)x * g.sb + (zq - g.zb0);
-        pa = a.a_b + (zq - g.zb0); pb = a.b_b + (zq - g.zb0);
+        ps4 = psi[3] + (size_t)x * g.sb + (zq - g.zb0);
+        pa = prof[6] + (zq - g.zb0); pb = prof[7] + (zq - g.zb0);
     }
-    const T *u = a.u + (size_t)x * P + zq;
+    const T *u = u0 + (size_t)x * P + zq;
     T q[12], ps[4];
     {
         T a0[4], a1[4], a2[4];
@@ -291,7 +292,12 @@ __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> 
 #pragma unroll
         for (int j = 0; j < 4; ++j) { q[j] = a0[j]; q[4 + j] = a1[j]; q[8 + j] = a2[j]; }
     }
-    ld4(psi, ps);
+    if (fresh) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ps[j] = (T)0;
+    } else {
+        ld4(ps4, ps);
+    }
     const float4 av = *reinterpret_cast<const float4 *>(pa);
     const float4 bv = *reinterpret_cast<const float4 *>(pb);
     const float aa[4] = {av.x, av.y, av.z, av.w}, bb[4] = {bv.x, bv.y, bv.z, bv.w};
@@ -300,8 +306,23 @@ __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> 
         const int z = zq + j;
         if (z >= zlo && z < zhi) ps[j] = (T)bb[j] * ps[j] + (T)aa[j] * dpsi_z<T>(q, j) * h1;
     }
-    st4(psi, ps);
+    st4(ps4, ps);
 }
+
+// Plain-plan psi kernel (blockIdx.y = strip).  With programmatic dependent launch it first
+// waits for the previous step kernel (whose output u_n it reads), then lets the next step
+// kernel start.
+template <typename T>
+__global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> a)
+{
+    griddep_wait();
+    griddep_launch();
+    T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
+    const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
+    psi_quad<T>(a.g, a.h1, a.u, psi, prof, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, false);
+}
+
+#include "rtm_batch.cuh"
 
 // ---- set-up and layout kernels ------------------------------------------------------------
 template <typename T>
@@ -576,6 +597,80 @@ cudaError_t launch_xcorr(const Geom &g, const T *src, const T *rcv, double *img,
     k_xcorr<T><<<grid, 128, 0, s>>>(g, src, rcv, img, slf);
     return cudaGetLastError();
 }
+
+void psi_counts_host(const Geom &g, int (&n)[4]) { psi_counts(g, n); }
+
+template <typename T>
+cudaError_t launch_bpsi(const BatchIndex *ix, const BMember<T> *mem, const int2 *state, int grid,
+                        int pdl, cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute at = pdl_attr();
+    cfg.attrs = pdl ? &at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    static cudaError_t carve = cudaFuncSetAttribute(k_bpsi<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                    cudaSharedmemCarveoutMaxShared);
+    if (carve != cudaSuccess) return carve;
+    return cudaLaunchKernelEx(&cfg, k_bpsi<T>, ix, mem, state);
+}
+
+constexpr int kBatchWarps = 8;
+
+template <typename T>
+static cudaError_t configure_bstep()
+{
+    static cudaError_t state = cudaErrorNotReady;
+    if (state == cudaErrorNotReady) {
+        state = cudaFuncSetAttribute(k_bstep<T, kBatchWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)StepCfg<T, kBatchWarps, 1>::SMEM);
+        if (state == cudaSuccess)
+            state = cudaFuncSetAttribute(k_bstep<T, kBatchWarps>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         cudaSharedmemCarveoutMaxShared);
+    }
+    return state;
+}
+
+template <typename T>
+int bstep_grid()
+{
+    static int grid = 0;
+    if (grid == 0) {
+        if (configure_bstep<T>() != cudaSuccess) return 0;
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bstep<T, kBatchWarps>, kBatchWarps * 32,
+                                                      StepCfg<T, kBatchWarps, 1>::SMEM);
+        grid = (per_sm < 1 ? 1 : per_sm) * sms;
+    }
+    return grid;
+}
+
+template <typename T>
+cudaError_t launch_bstep(const BatchIndex *ix, const BMember<T> *mem, int2 *state, unsigned *done,
+                         int grid, int pdl, cudaStream_t s)
+{
+    cudaError_t e = configure_bstep<T>();
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kBatchWarps * 32);
+    cfg.dynamicSmemBytes = StepCfg<T, kBatchWarps, 1>::SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute at = pdl_attr();
+    cfg.attrs = pdl ? &at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_bstep<T, kBatchWarps>, ix, mem, state, done);
+}
+
+template cudaError_t launch_bpsi<float>(const BatchIndex *, const BMember<float> *, const int2 *, int, int,
+                                        cudaStream_t);
+template cudaError_t launch_bstep<float>(const BatchIndex *, const BMember<float> *, int2 *, unsigned *,
+                                         int, int, cudaStream_t);
+template int bstep_grid<float>();
 
 #define RTM_INSTANTIATE(T)                                                                      \
     template cudaError_t launch_step<T>(int, const StepMaps &, const StepArgs<T> &, int, int,  \

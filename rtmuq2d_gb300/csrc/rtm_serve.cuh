@@ -1,0 +1,427 @@
+// rtm_serve.cuh -- serving and batching engine (host side; included at the end of
+// rtm_engine.cu, whose plan helpers it uses).
+//
+// A server holds up to kMaxMembers resident migrations ("members").  Requests are admitted
+// in arrival order while a member slot is free and their device footprint fits the HBM
+// budget; admission uploads the inputs and sets the member up (coef, seismogram transpose,
+// zeroed wavefields and image accumulators).  rtm_server_step replays a CUDA graph of
+// `steps_per_launch` batched time steps (k_bpsi + k_bstep per step, chained by programmatic
+// dependent launch): every active member advances one step per batched step, whatever its
+// grid, time axis or pass.  Members that finished their backward pass are harvested (image
+// and self image copied to host buffers) and their slots freed for the next admissions --
+// continuous batching.  One thread drives a server; each server has its own stream.
+
+namespace rtm {
+
+struct ServeRequest {
+    long long id;
+    rtm_params p;
+    std::vector<float> vel, wav, seis;     // host copies of the inputs
+    double t_submit, t_admit, t_done;
+    std::vector<float> img, slf;
+    long long bytes;
+};
+
+}  // namespace rtm
+
+struct rtm_server {
+    long long budget = 0, in_use = 0;
+    int max_members = rtm::kMaxMembers;
+    int steps_per_launch = 16;
+    cudaStream_t stream = nullptr;
+    // device side
+    rtm::BatchIndex *d_ix = nullptr;
+    rtm::BMember<float> *d_mem = nullptr;
+    int2 *d_state = nullptr;
+    unsigned *d_done = nullptr;
+    // host mirrors
+    std::vector<rtm::BMember<float>> mem;
+    rtm::BatchIndex ix;
+    int2 *h_state = nullptr;               // pinned
+    std::vector<rtm_plan *> slot_plan;     // plan backing each slot (nullptr: free)
+    std::vector<rtm::ServeRequest *> slot_req;
+    std::vector<rtm_plan *> idle;          // finished plans kept for reuse
+    std::deque<rtm::ServeRequest *> queue;
+    std::map<long long, rtm::ServeRequest *> done;
+    long long next_id = 1;
+    cudaGraphExec_t gexec = nullptr;
+    long long cell_updates_done = 0;
+    long long launches = 0;
+    double busy_ms = 0.0;                  // GPU time of the replays (events)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+};
+
+namespace rtm {
+
+static double now_s()
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+static void member_from_plan(rtm_plan *P, BMember<float> &M)
+{
+    memset(&M, 0, sizeof M);
+    M.tm_u[0] = P->tm_u[0]; M.tm_u[1] = P->tm_u[1];
+    M.tm_up[0] = P->tm_up[0]; M.tm_up[1] = P->tm_up[1];
+    M.tm_r[0] = P->tm_r[0]; M.tm_r[1] = P->tm_r[1];
+    M.tm_rp[0] = P->tm_rp[0]; M.tm_rp[1] = P->tm_rp[1];
+    M.tm_c = P->tm_c;
+    M.g = P->g;
+    const float dx = P->p.dx;
+    M.h1 = 1.0f / dx;
+    M.h2 = dx * dx;
+    M.h3 = 1.0f / (dx * dx);
+    M.u[0] = P->at<float>(P->L.u[0]); M.u[1] = P->at<float>(P->L.u[1]);
+    M.r[0] = P->at<float>(P->L.r[0]); M.r[1] = P->at<float>(P->L.r[1]);
+    for (int k = 0; k < 4; ++k) {
+        M.psi[k] = P->at<float>(P->L.psi[k]);
+        M.xi[k] = P->at<float>(P->L.xi[k]);
+    }
+    const float *prof = P->at<float>(P->L.prof);
+    const ProfLayout pl = prof_layout(P->g);
+    for (int k = 0; k < 8; ++k) M.prof[k] = prof + pl.off[k];
+    const int *rec = P->at<int>(P->L.rec);
+    M.rec_last = rec; M.rec_first = rec + P->g.dimx; M.rec_cnt = rec + 2 * P->g.dimx;
+    M.wav = P->at<float>(P->L.wav);
+    M.seis_t = P->at<float>(P->L.seis_t);
+    M.img = P->at<double>(P->L.img);
+    M.slf = P->at<double>(P->L.slf);
+    M.store = P->base + P->L.store;
+    M.slot_elems = P->L.slot_elems;
+    M.scales = P->p.precision == RTM_PREC_FP32 ? nullptr : P->at<float>(P->L.scales);
+    M.store_prec = P->p.precision;
+    M.storage = P->p.storage;
+    M.status = P->at<unsigned>(P->L.status);
+}
+
+static int server_fail(rtm_server *S, int code)
+{
+    S->err = rtm_last_error();
+    return code;
+}
+
+// Work lists of the current membership (inactive slots own no tiles).
+static void rebuild_index(rtm_server *S)
+{
+    S->ix.nmem = S->max_members;
+    int tb = 0, pb = 0;
+    for (int m = 0; m < S->max_members; ++m) {
+        S->ix.tile_base[m] = tb;
+        S->ix.psi_base[m] = pb;
+        if (S->slot_plan[m]) {
+            const Geom &g = S->slot_plan[m]->g;
+            int n[4];
+            psi_counts_host(g, n);
+            tb += g.tiles;
+            pb += n[0] + n[1] + n[2] + n[3];
+        }
+    }
+    S->ix.tile_base[S->max_members] = tb;
+    S->ix.psi_base[S->max_members] = pb;
+}
+
+// Sets up one admitted request in slot m on the server's stream.
+static int admit(rtm_server *S, int m, ServeRequest *R)
+{
+    rtm_plan *P = nullptr;
+    for (size_t i = 0; i < S->idle.size(); ++i)
+        if (same_params(S->idle[i]->p, R->p)) {
+            P = S->idle[i];
+            S->idle.erase(S->idle.begin() + i);
+            break;
+        }
+    if (!P) {
+        // make room: drop reusable plans that do not match
+        while (!S->idle.empty() && S->in_use + R->bytes > S->budget) {
+            S->in_use -= (long long)S->idle.back()->L.total;
+            plan_free(S->idle.back());
+            S->idle.pop_back();
+        }
+        RTM_TRY(plan_alloc(R->p, &P));
+        S->in_use += (long long)P->L.total;
+        RTM_CUDA(cudaStreamSynchronize(P->stream));
+        if (P->own_stream) cudaStreamDestroy(P->stream);
+        P->stream = S->stream;
+        P->own_stream = false;
+    }
+    const Geom &g = P->g;
+    cudaStream_t s = S->stream;
+    float *stage = P->at<float>(P->L.staging);
+    float *h;
+    RTM_TRY(pinned(P, std::max(R->vel.size(), R->seis.size()) * sizeof(float), &h));
+    RTM_CUDA(cudaStreamSynchronize(s));
+    memcpy(h, R->vel.data(), R->vel.size() * sizeof(float));
+    RTM_CUDA(cudaMemcpyAsync(stage, h, R->vel.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    RTM_CUDA(launch_coef<float>(g, stage, g.dimz, P->at<float>(P->L.coef), P->p.dx, P->p.dt, s));
+    if (g.nwav > 0)
+        RTM_CUDA(cudaMemcpyAsync(P->at<float>(P->L.wav), R->wav.data(), sizeof(float) * g.nwav,
+                                 cudaMemcpyHostToDevice, s));
+    if (g.nrec > 0) {
+        RTM_CUDA(cudaStreamSynchronize(s));     // staging and the pinned buffer are reused
+        memcpy(h, R->seis.data(), R->seis.size() * sizeof(float));
+        RTM_CUDA(cudaMemcpyAsync(stage, h, R->seis.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        RTM_CUDA(launch_transpose(stage, P->at<float>(P->L.seis_t), g.nrec, g.nt, s));
+    }
+    const size_t field = (size_t)g.dimx * g.pitch * sizeof(float);
+    for (int k = 0; k < 2; ++k) {
+        RTM_CUDA(cudaMemsetAsync(P->base + P->L.u[k], 0, field, s));
+        RTM_CUDA(cudaMemsetAsync(P->base + P->L.r[k], 0, field, s));
+    }
+    // psi/xi cells outside the updated ranges are read by the stencils as zero; the updated
+    // ones restart from zero at each pass (F_STRIPS_FRESH)
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.strips, 0, P->L.strip_bytes, s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.img, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.slf, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
+    RTM_CUDA(cudaMemsetAsync(P->base + P->L.status, 0, 256, s));
+    member_from_plan(P, S->mem[m]);
+    RTM_CUDA(cudaMemcpyAsync(S->d_mem + m, &S->mem[m], sizeof(BMember<float>), cudaMemcpyHostToDevice, s));
+    const int2 st = make_int2(1, 0);
+    RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &st, sizeof st, cudaMemcpyHostToDevice, s));
+    RTM_CUDA(cudaStreamSynchronize(s));         // host copies above come from stack/host data
+    S->slot_plan[m] = P;
+    S->slot_req[m] = R;
+    R->t_admit = now_s();
+    return RTM_OK;
+}
+
+static int harvest(rtm_server *S, int m)
+{
+    rtm_plan *P = S->slot_plan[m];
+    ServeRequest *R = S->slot_req[m];
+    const Geom &g = P->g;
+    const size_t n = (size_t)g.nx * g.nz;
+    float *stage = P->at<float>(P->L.staging);
+    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.img), stage, 0, S->stream));
+    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.slf), stage + n, 0, S->stream));
+    R->img.resize(n);
+    R->slf.resize(n);
+    float *h;
+    RTM_TRY(pinned(P, 2 * n * sizeof(float), &h));
+    RTM_CUDA(cudaMemcpyAsync(h, stage, 2 * n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+    unsigned st = 0;
+    RTM_CUDA(cudaMemcpyAsync(&st, P->base + P->L.status, sizeof st, cudaMemcpyDeviceToHost, S->stream));
+    const int2 idle_state = make_int2(0, 0);
+    RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &idle_state, sizeof idle_state, cudaMemcpyHostToDevice, S->stream));
+    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    memcpy(R->img.data(), h, n * sizeof(float));
+    memcpy(R->slf.data(), h + n, n * sizeof(float));
+    R->t_done = now_s();
+    S->cell_updates_done += 2LL * g.dimx * g.dimz * g.nt;
+    S->done[R->id] = R;
+    S->slot_plan[m] = nullptr;
+    S->slot_req[m] = nullptr;
+    S->idle.push_back(P);
+    if (st) return fail(RTM_ERR_TIMEOUT, "a tile load of request %lld timed out", R->id);
+    return RTM_OK;
+}
+
+static int capture_graph(rtm_server *S)
+{
+    const int grid = bstep_grid<float>();
+    if (grid < 1) return fail(RTM_ERR_CUDA, "batched step kernel cannot be configured");
+    int dev = 0, sms = 0;
+    RTM_CUDA(cudaGetDevice(&dev));
+    RTM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int pgrid = 4 * sms;
+    RTM_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < S->steps_per_launch && e == cudaSuccess; ++k) {
+        e = launch_bpsi<float>(S->d_ix, S->d_mem, S->d_state, pgrid, k > 0, S->stream);
+        if (e == cudaSuccess) e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, 1, S->stream);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(S->stream, &graph);
+    if (e != cudaSuccess || ec != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(RTM_ERR_CUDA, "batch graph capture: %s",
+                    cudaGetErrorString(e != cudaSuccess ? e : ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&S->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        S->gexec = nullptr;
+        return fail(RTM_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ei));
+    }
+    return RTM_OK;
+}
+
+}  // namespace rtm
+
+extern "C" {
+
+int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per_launch,
+                      rtm_server **out)
+{
+    if (!out) return fail(RTM_ERR_INVALID, "null argument");
+    if (max_members < 1 || max_members > kMaxMembers)
+        return fail(RTM_ERR_INVALID, "max_members must be in [1, %d]", kMaxMembers);
+    if (steps_per_launch < 1 || steps_per_launch > 256)
+        return fail(RTM_ERR_INVALID, "steps_per_launch must be in [1, 256]");
+    std::unique_ptr<rtm_server> S(new rtm_server());
+    S->max_members = max_members;
+    S->steps_per_launch = steps_per_launch;
+    if (hbm_budget_bytes <= 0) {
+        size_t fr = 0, tot = 0;
+        RTM_CUDA(cudaMemGetInfo(&fr, &tot));
+        hbm_budget_bytes = (long long)(0.8 * (double)fr);
+    }
+    S->budget = hbm_budget_bytes;
+    RTM_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    RTM_CUDA(cudaMalloc(&S->d_ix, sizeof(BatchIndex)));
+    RTM_CUDA(cudaMalloc(&S->d_mem, sizeof(BMember<float>) * kMaxMembers));
+    RTM_CUDA(cudaMalloc(&S->d_state, sizeof(int2) * kMaxMembers));
+    RTM_CUDA(cudaMalloc(&S->d_done, 2 * sizeof(unsigned)));
+    RTM_CUDA(cudaMallocHost(&S->h_state, sizeof(int2) * kMaxMembers));
+    RTM_CUDA(cudaMemsetAsync(S->d_state, 0, sizeof(int2) * kMaxMembers, S->stream));
+    RTM_CUDA(cudaMemsetAsync(S->d_done, 0, 2 * sizeof(unsigned), S->stream));
+    RTM_CUDA(cudaEventCreate(&S->ev0));
+    RTM_CUDA(cudaEventCreate(&S->ev1));
+    S->mem.resize(kMaxMembers);
+    S->slot_plan.assign(max_members, nullptr);
+    S->slot_req.assign(max_members, nullptr);
+    memset(&S->ix, 0, sizeof S->ix);
+    rebuild_index(S.get());
+    RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
+    RTM_TRY(capture_graph(S.get()));
+    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    *out = S.release();
+    return RTM_OK;
+}
+
+int rtm_server_destroy(rtm_server *S)
+{
+    if (!S) return RTM_OK;
+    cudaStreamSynchronize(S->stream);
+    for (rtm_plan *P : S->slot_plan) if (P) plan_free(P);
+    for (rtm_plan *P : S->idle) plan_free(P);
+    for (auto *R : S->slot_req) delete R;
+    for (auto *R : S->queue) delete R;
+    for (auto &kv : S->done) delete kv.second;
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    cudaFree(S->d_ix); cudaFree(S->d_mem); cudaFree(S->d_state); cudaFree(S->d_done);
+    cudaFreeHost(S->h_state);
+    cudaEventDestroy(S->ev0); cudaEventDestroy(S->ev1);
+    cudaStreamDestroy(S->stream);
+    delete S;
+    return RTM_OK;
+}
+
+int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
+                      const float *seismogram, long long *request_id)
+{
+    if (!S || !p || !velocity) return fail(RTM_ERR_INVALID, "null argument");
+    RTM_TRY(check_params(*p));
+    if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "the server runs FP32 migrations");
+    const long long bytes = rtm_footprint_bytes(p);
+    if (bytes > S->budget) return fail(RTM_ERR_NOMEM, "request needs %lld bytes, budget %lld", bytes, S->budget);
+    auto *R = new ServeRequest();
+    R->id = S->next_id++;
+    R->p = *p;
+    const size_t nv = (size_t)(p->th_left + p->nx + p->th_right) * (p->th_up + p->nz + p->th_down);
+    R->vel.assign(velocity, velocity + nv);
+    if (p->n_wavelet > 0) R->wav.assign(wavelet, wavelet + p->n_wavelet);
+    if (p->rec_count > 0) R->seis.assign(seismogram, seismogram + (size_t)p->rec_count * p->nt);
+    R->bytes = bytes;
+    R->t_submit = now_s();
+    S->queue.push_back(R);
+    if (request_id) *request_id = R->id;
+    return RTM_OK;
+}
+
+// Admits what fits, runs steps_per_launch batched steps, harvests finished members.
+int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null server");
+    bool changed = false;
+    // admission in arrival order (head of line blocks: requests are served FIFO)
+    while (!S->queue.empty()) {
+        ServeRequest *R = S->queue.front();
+        int slot = -1;
+        for (int m = 0; m < S->max_members; ++m)
+            if (!S->slot_plan[m]) { slot = m; break; }
+        if (slot < 0) break;
+        bool reusable = false;
+        for (rtm_plan *P : S->idle) if (same_params(P->p, R->p)) reusable = true;
+        long long idle_bytes = 0;
+        for (rtm_plan *P : S->idle) idle_bytes += (long long)P->L.total;
+        if (!reusable && S->in_use - idle_bytes + R->bytes > S->budget) break;
+        const int st = admit(S, slot, R);
+        if (st != RTM_OK) return st;
+        S->queue.pop_front();
+        changed = true;
+    }
+    if (changed) {
+        rebuild_index(S);
+        RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
+    }
+    int active = 0;
+    for (int m = 0; m < S->max_members; ++m) active += S->slot_plan[m] != nullptr;
+    if (active > 0) {
+        RTM_CUDA(cudaEventRecord(S->ev0, S->stream));
+        RTM_CUDA(cudaGraphLaunch(S->gexec, S->stream));
+        RTM_CUDA(cudaEventRecord(S->ev1, S->stream));
+        S->launches += 2LL * S->steps_per_launch;
+        RTM_CUDA(cudaMemcpyAsync(S->h_state, S->d_state, sizeof(int2) * S->max_members,
+                                 cudaMemcpyDeviceToHost, S->stream));
+        RTM_CUDA(cudaStreamSynchronize(S->stream));
+        float ms = 0.0f;
+        RTM_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
+        S->busy_ms += ms;
+        unsigned flags[2] = {0, 0};
+        RTM_CUDA(cudaMemcpy(flags, S->d_done, sizeof flags, cudaMemcpyDeviceToHost));
+        if (flags[1]) return fail(RTM_ERR_TIMEOUT, "a batched tile load timed out");
+        bool freed = false;
+        for (int m = 0; m < S->max_members; ++m)
+            if (S->slot_plan[m] && S->h_state[m].x == 3) {
+                RTM_TRY(harvest(S, m));
+                freed = true;
+            }
+        if (freed) {
+            rebuild_index(S);
+            RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
+        }
+    }
+    if (n_active) {
+        int a = 0;
+        for (int m = 0; m < S->max_members; ++m) a += S->slot_plan[m] != nullptr;
+        *n_active = a;
+    }
+    if (n_queued) *n_queued = (int)S->queue.size();
+    return RTM_OK;
+}
+
+// Takes one finished request, if any: RTM_BUSY when none is ready.  image / self_image
+// (nx x nz, may be NULL) receive the result; times (may be NULL) get the submit, admit and
+// finish times in seconds on a monotonic clock.
+int rtm_server_poll(rtm_server *S, long long *request_id, float *image, float *self_image,
+                    double *times)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null server");
+    if (S->done.empty()) return RTM_ERR_BUSY;
+    auto it = S->done.begin();
+    ServeRequest *R = it->second;
+    if (request_id) *request_id = R->id;
+    if (image) memcpy(image, R->img.data(), R->img.size() * sizeof(float));
+    if (self_image) memcpy(self_image, R->slf.data(), R->slf.size() * sizeof(float));
+    if (times) { times[0] = R->t_submit; times[1] = R->t_admit; times[2] = R->t_done; }
+    S->done.erase(it);
+    delete R;
+    return RTM_OK;
+}
+
+// Totals since creation: credited cell-updates of finished requests, GPU milliseconds of
+// the batched steps, kernel launches, device bytes held.
+int rtm_server_stats(const rtm_server *S, long long *cell_updates, double *gpu_ms, long long *launches,
+                     long long *bytes_in_use)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null server");
+    if (cell_updates) *cell_updates = S->cell_updates_done;
+    if (gpu_ms) *gpu_ms = S->busy_ms;
+    if (launches) *launches = S->launches;
+    if (bytes_in_use) *bytes_in_use = S->in_use;
+    return RTM_OK;
+}
+
+}  // extern "C"

@@ -89,7 +89,7 @@ __device__ __forceinline__ T d2z_q(const T (&zz)[12], int j)
 template <typename T>
 __device__ __forceinline__ void cpml_x_quad(const T *psi, T *xi, size_t P, T ab, T bb, const T (&W)[9][4],
                                             const T (&cf)[4], T (&v)[4], int zq, int zlo, int zhi,
-                                            T h1, T h2, T h3)
+                                            T h1, T h2, T h3, bool fresh)
 {
     // dpsi = B4 (f+4 - f-4) + B3 (f+3 - f-3) + B2 (f+2 - f-2) + B1 (f+1 - f-1), one row pair
     // at a time (same operand order as absorbingBoundaryCondition.c:198-203)
@@ -109,7 +109,12 @@ __device__ __forceinline__ void cpml_x_quad(const T *psi, T *xi, size_t P, T ab,
         }
     }
     T x4[4];
-    ld4(xi, x4);
+    if (fresh) {                          // first step of a pass: xi starts from zero
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
+    } else {
+        ld4(xi, x4);
+    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int z = zq + j;
@@ -128,7 +133,7 @@ __device__ __forceinline__ void cpml_x_quad(const T *psi, T *xi, size_t P, T ab,
 template <typename T>
 __device__ __forceinline__ void cpml_z_quad(const T *psi, T *xi, const float *ab, const float *bb,
                                             const T (&zz)[12], const T (&cf)[4], T (&v)[4], int zq,
-                                            int zlo, int zhi, T h1, T h2, T h3)
+                                            int zlo, int zhi, T h1, T h2, T h3, bool fresh)
 {
     T q[12];
     {
@@ -140,7 +145,12 @@ __device__ __forceinline__ void cpml_z_quad(const T *psi, T *xi, const float *ab
         for (int j = 0; j < 4; ++j) { q[j] = a0[j]; q[4 + j] = a1[j]; q[8 + j] = a2[j]; }
     }
     T x4[4];
-    ld4(xi, x4);
+    if (fresh) {                          // first step of a pass: xi starts from zero
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
+    } else {
+        ld4(xi, x4);
+    }
     const float4 av = *reinterpret_cast<const float4 *>(ab);
     const float4 bv = *reinterpret_cast<const float4 *>(bb);
     const float aa[4] = {av.x, av.y, av.z, av.w}, bbv[4] = {bv.x, bv.y, bv.z, bv.w};
@@ -183,6 +193,7 @@ __device__ __forceinline__ void cpml_quad_all(const StepArgs<T> &a, const T *su,
     const bool inT = zq + 4 > 4 && zq < g.thu - 4;               // every column (the quirk)
     const bool inB = x >= 4 && x < g.dimx - 4 && zq + 4 > g.dimz - g.thd + 4 && zq < g.dimz - 4;
     if (!(inL || inR || inT || inB)) return;
+    const bool fresh = (a.flags & F_STRIPS_FRESH) != 0;
     T v[4], cf[4];
     ld4(O + c * TZ + 4 * qi, v);
     ld4(scf + c * TZ + 4 * qi, cf);
@@ -193,24 +204,24 @@ __device__ __forceinline__ void cpml_quad_all(const StepArgs<T> &a, const T *su,
         for (int m = 0; m < 9; ++m) ld4(col + (m - 4) * SZ, W[m]);
         if (inL)
             cpml_x_quad<T>(a.psi_l + (size_t)x * P + zq, a.xi_l + (size_t)x * P + zq, P, (T)a.a_l[x],
-                           (T)a.b_l[x], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3);
+                           (T)a.b_l[x], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
         if (inT) {
             T zz[12];
             z_line<T>(su, c + HALO, 4 * qi + HALO, W[4], zz);
             cpml_z_quad<T>(a.psi_t + (size_t)x * g.st + zq, a.xi_t + (size_t)x * g.st + zq, a.a_t + zq,
-                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3);
+                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3, fresh);
         }
         if (inR) {
             const int li = x - (g.dimx - g.thr);
             cpml_x_quad<T>(a.psi_r + (size_t)li * P + zq, a.xi_r + (size_t)li * P + zq, P, (T)a.a_r[li],
-                           (T)a.b_r[li], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3);
+                           (T)a.b_r[li], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
         }
         if (inB) {
             T zz[12];
             z_line<T>(su, c + HALO, 4 * qi + HALO, W[4], zz);
             const int lq = zq - g.zb0;
             cpml_z_quad<T>(a.psi_b + (size_t)x * g.sb + lq, a.xi_b + (size_t)x * g.sb + lq, a.a_b + lq,
-                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3);
+                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
         }
     } else {
         T c4[4], zz[12];
@@ -218,11 +229,11 @@ __device__ __forceinline__ void cpml_quad_all(const StepArgs<T> &a, const T *su,
         z_line<T>(su, c + HALO, 4 * qi + HALO, c4, zz);
         if (inT)
             cpml_z_quad<T>(a.psi_t + (size_t)x * g.st + zq, a.xi_t + (size_t)x * g.st + zq, a.a_t + zq,
-                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3);
+                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3, fresh);
         if (inB) {
             const int lq = zq - g.zb0;
             cpml_z_quad<T>(a.psi_b + (size_t)x * g.sb + lq, a.xi_b + (size_t)x * g.sb + lq, a.a_b + lq,
-                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3);
+                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
         }
     }
     st4(O + c * TZ + 4 * qi, v);

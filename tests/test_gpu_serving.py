@@ -1,0 +1,107 @@
+"""Serving / batching engine (rtm_server_*): resident migrations advanced together by the
+batched step kernels must give the same images as one migration run alone through
+rtm_migrate_shot (same tiles, same arithmetic: bit-identical), whatever the mix they run in.
+"""
+import numpy as np
+import pytest
+
+from golden_util import case_params, load, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(eng, d, name, **kw):
+    p = eng.RtmParams.make(**case_params(d, name)).replace(**kw)
+    return p, d[name + "/ext"], d[name + "/wavelet"], d[name + "/seis"]
+
+
+def _shorter(eng, case, nt):
+    p, ext, wav, seis = case
+    return p.replace(nt=nt), ext, wav, np.ascontiguousarray(seis[:, :nt])
+
+
+def _mix(eng, d):
+    """Different grids, time axes, storages and storage precisions."""
+    cases = [_case(eng, d, "uneven", storage=1),
+             _case(eng, d, "quirks", storage=0),
+             _case(eng, d, "uneven", storage=0, precision=1),
+             _case(eng, d, "uneven", storage=1, precision=2)]
+    cases.append(_shorter(eng, cases[0], cases[0][0].nt - 37))
+    cases.append(_shorter(eng, cases[1], cases[1][0].nt // 2 + 3))
+    return cases
+
+
+@pytest.mark.parametrize("name", ("uneven", "quirks"))
+@pytest.mark.parametrize("storage", (0, 1))
+def test_server_single_request_equals_migrate_shot(engine, name, storage):
+    d = load()
+    p, ext, wav, seis = _case(engine, d, name, storage=storage)
+    try:
+        engine.params_check(p)
+    except engine.RtmError:
+        pytest.skip("shot outside the reconstruction region for this case")
+    ref_img, ref_slf = engine.migrate_shot(p, ext, wav, seis)
+    srv = engine.Server(0, max_members=4, steps_per_launch=16)
+    rid = srv.submit(p, ext, wav, seis)
+    out = srv.run_all()
+    img, slf, times = out[rid]
+    srv.close()
+    assert np.array_equal(img, ref_img)
+    assert np.array_equal(slf, ref_slf)
+    assert rel_l2(img, d[name + "/image"]) <= 1e-4
+    assert times[0] <= times[1] <= times[2]
+
+
+def test_server_mixed_batch_equals_each_alone(engine):
+    d = load()
+    cases = [c for c in _mix(engine, d) if _valid(engine, c[0])]
+    solo = [engine.migrate_shot(*c) for c in cases]
+    # fewer slots than requests: members finish and new ones are admitted mid-run;
+    # steps_per_launch not dividing any nt: members finish inside a graph replay
+    srv = engine.Server(0, max_members=3, steps_per_launch=7)
+    ids = [srv.submit(*c) for c in cases]
+    out = srv.run_all()
+    st = srv.stats()
+    srv.close()
+    for rid, (img, slf) in zip(ids, solo):
+        assert np.array_equal(out[rid][0], img), rid
+        assert np.array_equal(out[rid][1], slf), rid
+    assert st["cell_updates"] == sum(c[0].cell_updates for c in cases)
+    assert st["gpu_ms"] > 0 and st["launches"] > 0
+
+
+def test_server_admission_respects_budget(engine):
+    d = load()
+    cases = [_case(engine, d, "uneven", storage=1) for _ in range(3)]
+    fp = engine.footprint_bytes(cases[0][0])
+    srv = engine.Server(int(fp * 1.5), max_members=8, steps_per_launch=32)
+    ids = [srv.submit(*c) for c in cases]
+    seen = []
+    out = {}
+    while len(out) < len(ids):
+        active, queued = srv.step()
+        seen.append(active)
+        r = srv.poll()
+        while r is not None:
+            out[r[0]] = r[1:]
+            r = srv.poll()
+    assert max(seen) == 1                     # one footprint fits the budget at a time
+    assert srv.stats()["bytes_in_use"] <= int(fp * 1.5)
+    ref, _ = engine.migrate_shot(*cases[0])
+    for rid in ids:
+        assert np.array_equal(out[rid][0], ref)
+    big = cases[0][0].replace(nx=cases[0][0].nx * 4)
+    with pytest.raises(engine.RtmError):
+        srv.submit(big, np.zeros((big.dim_x, big.dim_z), np.float32), cases[0][2],
+                   np.zeros((big.rec_count, big.nt), np.float32))
+    with pytest.raises(engine.RtmError):
+        srv.submit(cases[0][0].replace(compute=1), *cases[0][1:])
+    srv.close()
+
+
+def _valid(engine, p):
+    try:
+        engine.params_check(p)
+        return True
+    except engine.RtmError:
+        return False
