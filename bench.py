@@ -50,6 +50,17 @@ def parse():
                     help="profiling only: shorten the time axis (the reported workload changes)")
     ap.add_argument("--quick", action="store_true",
                     help="profiling only: device-resident timing, no e2e or CPU baseline")
+    ap.add_argument("--batch-members", type=int, default=64,
+                    help="batched UQ ensemble: velocity realizations (0: skip)")
+    ap.add_argument("--batch-nt", type=int, default=7500)
+    ap.add_argument("--plain-sample", type=int, default=6,
+                    help="ensemble members also run one at a time through the plain path")
+    ap.add_argument("--serve-requests", type=int, default=96,
+                    help="serving trace: Poisson-arriving requests (0: skip)")
+    ap.add_argument("--serve-load", type=float, default=0.8,
+                    help="arrival rate as a fraction of the batched service capacity")
+    ap.add_argument("--steps-per-launch", type=int, default=16,
+                    help="batched steps per CUDA-graph replay of the server")
     return ap.parse_args()
 
 
@@ -213,6 +224,117 @@ def cpu_sample(p, ext, wav, seis, target_s, dtype=np.float32):
                       "(oracle/rtm_oracle.c, -O3 OpenMP)" % (p.dim_x, p.dim_z, nt, p.nt)}
 
 
+def run_batched(args, eng):
+    """The batched UQ ensemble through the serving engine: every member resident at once,
+    advanced together by the batched step kernels.  Timed from the first submit (host
+    buffers) to the last image on the host; a sample of the members is also run one at a
+    time through the plain path for the served-vs-plain ratio."""
+    from rtmuq2d_gb300 import workloads
+    members, true, mig = workloads.ensemble(args.batch_members, args.batch_nt)
+    wav = workloads.wavelet_for(members[0]["params"])
+    inputs = []
+    for m in members:
+        p = m["params"]
+        ext_true, ext = workloads.ensemble_inputs(m, true, mig)
+        seis = eng.model_seismogram(p.replace(storage=0), ext_true, wav)
+        inputs.append((p, ext, wav, seis))
+    cells = sum(p.cell_updates for p, *_ in inputs)
+    # plain path, one migration at a time (warm the plan cache with the first member)
+    sample = inputs[: max(0, min(args.plain_sample, len(inputs)))]
+    plain = None
+    plain_images = {}
+    if sample:
+        eng.migrate_shot(*sample[0])
+        t0 = time.perf_counter()
+        for i, inp in enumerate(sample):
+            plain_images[i] = eng.migrate_shot(*inp)[0]
+        dt = time.perf_counter() - t0
+        plain = sum(p.cell_updates for p, *_ in sample) / dt / 1e9
+    eng.release_cached()
+    srv = eng.Server(0, max_members=min(len(inputs), 128), steps_per_launch=args.steps_per_launch)
+    t0 = time.perf_counter()
+    ids = [srv.submit(*inp) for inp in inputs]
+    out = srv.run_all()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    agree = max((float(np.linalg.norm(out[ids[i]][0] - img) / max(np.linalg.norm(img), 1e-30))
+                 for i, img in plain_images.items()), default=None)
+    widths = [p.nx for p, *_ in inputs]
+    value = cells / wall / 1e9
+    return {"workload": "uq_ensemble_%dx_windows%d-%d_nz700_nt%d" % (len(inputs), min(widths),
+                                                                      max(widths), args.batch_nt),
+            "members": len(inputs), "value": value, "unit": "Gcell-updates/s",
+            "seconds": wall, "gpu_busy_value": cells / (st["gpu_ms"] * 1e-3) / 1e9,
+            "plain_value_same_members": plain, "plain_sample": len(sample),
+            "speedup_vs_plain": value / plain if plain else None,
+            "image_agreement_with_plain_rel_l2": agree,
+            "steps_per_launch": args.steps_per_launch, "device_bytes": st["bytes_in_use"],
+            "gpu_launches": st["launches"],
+            "timing": "wall clock from the first submit (host buffers) to the last image on the host"}
+
+
+def run_served(args, eng, capacity_gcells):
+    """The serving trace: Poisson arrivals of migrations of mixed grids, nt and ring
+    precision at `serve_load` x the batched capacity; latency = finish - arrival."""
+    from rtmuq2d_gb300 import synth, workloads
+    reqs = workloads.serving_trace(args.serve_requests)
+    templates = {}
+    for k in sorted({r["grid"] for r in reqs}):
+        p, true, mig = workloads.serving_template(k)
+        wav = workloads.wavelet_for(p)
+        ext_true = eng.extend_matrix(p, true)
+        seis = eng.model_seismogram(p.replace(storage=0), ext_true, wav)
+        templates[k] = (p, mig, wav, seis)
+    prepared = []
+    for r in reqs:
+        p0, mig, wav, seis = templates[r["grid"]]
+        p = p0.replace(nt=r["nt"], precision=r["precision"])
+        g = synth.grf_coarse((p.nx, p.nz), p.dx, 200.0, r["seed"])
+        ext = eng.extend_matrix(p, (mig.astype(np.float64) * np.exp(0.03 * g)).astype(np.float32))
+        prepared.append((p, ext, wav, np.ascontiguousarray(seis[:, : r["nt"]])))
+    mean_cells = float(np.mean([p.cell_updates for p, *_ in prepared]))
+    rate = args.serve_load * capacity_gcells * 1e9 / mean_cells          # requests / s
+    rng = np.random.default_rng(29)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(prepared)))
+    try:
+        total_hbm = eng.device_info()["hbm_bytes"]
+    except Exception:
+        total_hbm = None
+    srv = eng.Server(0, max_members=128, steps_per_launch=args.steps_per_launch)
+    done, occ, id_to_req = {}, [], {}
+    t_start = time.monotonic()
+    i = 0
+    while len(done) < len(prepared):
+        now = time.monotonic() - t_start
+        while i < len(prepared) and arrivals[i] <= now:
+            id_to_req[srv.submit(*prepared[i])] = i
+            i += 1
+        active, queued = srv.step()
+        occ.append(srv.stats()["bytes_in_use"])
+        r = srv.poll()
+        while r is not None:
+            done[id_to_req[r[0]]] = r[3][2]
+            r = srv.poll()
+        if active == 0 and queued == 0 and i < len(prepared):
+            time.sleep(max(0.0, min(0.002, arrivals[i] - (time.monotonic() - t_start))))
+    wall = time.monotonic() - t_start
+    st = srv.stats()
+    srv.close()
+    lat = np.array([done[k] - (t_start + arrivals[k]) for k in range(len(prepared))])
+    cells = sum(p.cell_updates for p, *_ in prepared)
+    return {"workload": "serving_trace_%d_requests" % len(prepared),
+            "requests": len(prepared), "value": cells / wall / 1e9, "unit": "Gcell-updates/s",
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "mean_latency_s": float(lat.mean()), "seconds": wall,
+            "arrival_rate_per_s": rate, "offered_load": args.serve_load,
+            "gpu_busy_value": cells / (st["gpu_ms"] * 1e-3) / 1e9,
+            "hbm_occupancy_mean": (float(np.mean(occ)) / total_hbm) if total_hbm else None,
+            "hbm_occupancy_max": (float(np.max(occ)) / total_hbm) if total_hbm else None,
+            "grids": [list(g) for g in workloads.SERVING_GRIDS], "nt_range": [2000, 7500],
+            "ring_precisions": ["fp32", "bf16"], "gpu_launches": st["launches"]}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -366,6 +488,18 @@ def run_gpu(args):
                 "fwd_kernel_achieved_gbs": nbytes["k_step_fwd"] / (fwd_avg_ms * 1e-3) / 1e9,
                 "note": "fields stream from HBM every step (warm-cache ncu: 37 MB read per "
                         "forward step, L2 hit rate 47%); traffic: cold-cache ncu reads"}
+    batched = served = None
+    if ws == 1 and args.batch_members > 0:
+        with ClockSampler(local) as smp:
+            batched = run_batched(args, eng)
+        batched["clocks"] = smp.summary()
+    if ws == 1 and args.serve_requests > 0:
+        cap = batched["value"] if batched else value
+        with ClockSampler(local) as smp:
+            served = run_served(args, eng, cap)
+        served["clocks"] = smp.summary()
+        served["plain_value"] = value
+        served["speedup_vs_plain"] = served["value"] / value
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
@@ -383,7 +517,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
                     "entry_point": "rtm_migrate_shot", "image_agreement_rel_l2": agree},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": sampler.summary()}
+            "clocks": sampler.summary(), "batched": batched, "served": served}
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

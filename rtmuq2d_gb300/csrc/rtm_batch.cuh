@@ -20,16 +20,6 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m)
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
 }
 
-__device__ __forceinline__ int find_member(const int *base, int n, int idx)
-{
-    int lo = 0, hi = n;                  // base[lo] <= idx < base[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (base[mid] <= idx) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
 // Number of psi quads of a member (the four strips of k_psi).
 __host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
 {
@@ -126,18 +116,25 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
                                               const BMember<T> *__restrict__ mem,
                                               const int2 *__restrict__ state)
 {
+    __shared__ int s_base[kMaxMembers + 1];
+    __shared__ int2 s_state[kMaxMembers];
     griddep_wait();
     griddep_launch();
-    const int n = ix->psi_base[ix->nmem];
+    const int nmem = ix->nmem;
+    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->psi_base[k];
+    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
+    __syncthreads();
+    const int n = s_base[nmem];
+    int m = 0;                                         // member of q (monotone in q)
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        const int m = find_member(ix->psi_base, ix->nmem, q);
-        const int2 st = state[m];                      // (pass, t)
+        while (s_base[m + 1] <= q) ++m;
+        const int2 st = s_state[m];                    // (pass, t)
         if (st.x != 1 && st.x != 2) continue;
         const BMember<T> &M = mem[m];
         const Geom &g = M.g;
         int cnt[4];
         psi_counts(g, cnt);
-        int lq = q - ix->psi_base[m], strip = 0;
+        int lq = q - s_base[m], strip = 0;
         while (strip < 3 && lq >= cnt[strip]) lq -= cnt[strip++];
         const T *u = st.x == 1 ? M.u[st.y & 1] : M.r[st.y & 1];
         const bool fresh = st.y == 0;
@@ -146,7 +143,7 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
 }
 
 template <typename T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 1)
+__global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2 : 1)
     k_bstep(const BatchIndex *__restrict__ ix, const BMember<T> *__restrict__ mem,
             int2 *__restrict__ state, unsigned *__restrict__ done)
 {
@@ -158,7 +155,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     __shared__ int tile_of[NS], pass_of[NS];
     __shared__ StepArgs<T> sargs[NS];
     __shared__ float red[WARPS];
-    const int total = ix->tile_base[ix->nmem];
+    // The work list and the members' (pass, step) of this launch, staged once: the tile ->
+    // member lookups of the issuing thread then stay in shared memory.  state[] is final
+    // here: k_bpsi of this step waited for the previous k_bstep before letting this grid
+    // launch, and the last CTA of this grid rewrites state[] only after every CTA is done.
+    __shared__ int s_base[kMaxMembers + 1];
+    __shared__ int2 s_state[kMaxMembers];
+    const int nmem = ix->nmem;
+    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->tile_base[k];
+    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
 
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -166,9 +171,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         fence_barrier_init();
     }
     __syncthreads();
+    const int total = s_base[nmem];
     // Thread 0 maps the i-th tile of this CTA to (member, local tile), builds the member's
-    // step arguments in shared memory and starts the stage's TMA loads.
-    int last_m = -1;
+    // step arguments in shared memory and starts the stage's TMA loads.  The tiles of a CTA
+    // visit the members in increasing order; all tiles of a member share its arguments, so
+    // they are built once per member and copied between stage slots.
+    int cur_m = 0;          // member of the latest tile (monotone)
+    int last_m = -1;        // member whose arguments sit in slot last_slot
+    int last_slot = 0;
+    int l_cur = 0, l_sc = 0, l_sp = 0;
     auto issue = [&](int i, int s) {
         const int tg = blockIdx.x + i * gridDim.x;
         if (tg >= total) {
@@ -176,8 +187,9 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             mbar_arrive(&full[s]);
             return;
         }
-        const int m = find_member(ix->tile_base, ix->nmem, tg);
-        const int2 st = state[m];
+        while (s_base[cur_m + 1] <= tg) ++cur_m;
+        const int m = cur_m;
+        const int2 st = s_state[m];
         if (st.x != 1 && st.x != 2) {     // idle or finished member: nothing to do
             tile_of[s] = -2;
             mbar_arrive(&full[s]);
@@ -191,28 +203,33 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             tensormap_acquire(&M.tm_r[0]); tensormap_acquire(&M.tm_r[1]);
             tensormap_acquire(&M.tm_rp[0]); tensormap_acquire(&M.tm_rp[1]);
             tensormap_acquire(&M.tm_c);
+            member_args<T>(M, st.x, st.y, sargs[s], l_cur, l_sc, l_sp);
             last_m = m;
+        } else if (last_slot != s) {
+            const int *src = reinterpret_cast<const int *>(&sargs[last_slot]);
+            int *dst = reinterpret_cast<int *>(&sargs[s]);
+#pragma unroll 8
+            for (int k = 0; k < (int)(sizeof(StepArgs<T>) / sizeof(int)); ++k) dst[k] = src[k];
         }
-        int cur, sc, sp;
-        member_args<T>(M, st.x, st.y, sargs[s], cur, sc, sp);
-        const int lt = tg - ix->tile_base[m];
+        last_slot = s;
+        const int lt = tg - s_base[m];
         tile_of[s] = lt;
         pass_of[s] = st.x;
-        const Geom &g = M.g;
+        const Geom &g = sargs[s].g;
         int xt, zt;
         tile_coords(g, lt, xt, zt);
         const int x0 = xt * TXC, z0 = ztile_origin(g, zt);
         const bool recon = st.x == 2 && (sargs[s].flags & F_RECON);
-        const CUtensorMap *mc = st.x == 1 ? &M.tm_u[cur] : &M.tm_r[cur];
-        const CUtensorMap *mp = st.x == 1 ? &M.tm_up[1 - cur] : &M.tm_rp[1 - cur];
+        const CUtensorMap *mc = st.x == 1 ? &M.tm_u[l_cur] : &M.tm_r[l_cur];
+        const CUtensorMap *mp = st.x == 1 ? &M.tm_up[1 - l_cur] : &M.tm_rp[1 - l_cur];
         T *stg = stage0 + (size_t)s * STAGE;
         mbar_arrive_expect_tx(&full[s], (uint32_t)(sizeof(T) * (recon ? 2 * UT + 3 * PT : UT + 2 * PT)));
         tma_load_2d(stg, mc, z0 - HALO, x0 - HALO, &full[s]);
         tma_load_2d(stg + UT, mp, z0, x0, &full[s]);
         tma_load_2d(stg + UT + PT, &M.tm_c, z0, x0, &full[s]);
         if (recon) {
-            tma_load_2d(stg + UT + 2 * PT, &M.tm_u[sc], z0 - HALO, x0 - HALO, &full[s]);
-            tma_load_2d(stg + 2 * UT + 2 * PT, &M.tm_up[sp], z0, x0, &full[s]);
+            tma_load_2d(stg + UT + 2 * PT, &M.tm_u[l_sc], z0 - HALO, x0 - HALO, &full[s]);
+            tma_load_2d(stg + 2 * UT + 2 * PT, &M.tm_up[l_sp], z0, x0, &full[s]);
         }
     };
     if (threadIdx.x == 0) {

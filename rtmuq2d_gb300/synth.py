@@ -105,3 +105,16 @@ def ensemble_member(model: np.ndarray, dx: float, seed: int, sigma: float = 0.03
                     corr_len: float = 200.0) -> np.ndarray:
     g = grf(model.shape, dx, corr_len, seed)
     return (model.astype(np.float64) * np.exp(sigma * g)).astype(np.float32)
+
+
+def grf_coarse(shape, dx: float, corr_len: float, seed: int, factor: int = 4) -> np.ndarray:
+    """grf() generated on a grid `factor` times coarser and interpolated (linear) back:
+    the same covariance to within the interpolation smoothing when corr_len spans many
+    cells, at a fraction of the cost on large grids."""
+    cs = tuple(max(2, -(-n // factor) + 1) for n in shape)
+    g = grf(cs, dx * factor, corr_len, seed)
+    zoom = tuple((n - 1) / (c - 1) for n, c in zip(shape, cs))
+    out = ndimage.zoom(g, zoom, order=1, mode="nearest", grid_mode=False)[: shape[0], : shape[1]]
+    out = out - out.mean()
+    sd = out.std()
+    return out / sd if sd > 0 else out

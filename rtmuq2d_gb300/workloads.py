@@ -73,3 +73,66 @@ def wavelet_for(p: RtmParams, f0: float | None = None) -> np.ndarray:
     if f0 is None:
         f0 = 15.0 if p.dt >= 1e-3 else 20.0
     return synth.ricker(f0, p.dt, max(p.n_wavelet, 1))[: max(p.n_wavelet, 1)]
+
+
+# ---- batched ensemble and serving trace -------------------------------------------------------
+def ensemble(n: int = 64, nt: int = 7500, seed: int = 11, storage: int = STORE_RING, precision: int = 0):
+    """The batched UQ ensemble: n velocity realizations of the 3400 x 700 faulted model, each
+    multiplied by exp(0.03 g_k) (g_k: independent unit Gaussian random field, 200 m
+    correlation), paired with one shot on an aperture window of width U[1200, 3400] cells
+    (full depth, 700).  The shot sits at the window centre, one receiver per window column.
+
+    Returns (members, true_model) with members a list of dicts: params, offset (first model
+    column of the window), seed."""
+    base = params_large(storage=storage, precision=precision, nt=nt)
+    true, mig = models_large(base, seed=1)
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        w = int(rng.integers(1200, 3401))
+        o = int(rng.integers(0, 3400 - w + 1))
+        p = base.replace(nx=w, shot_x=w // 2, rec_count=w)
+        out.append({"params": p, "offset": o, "seed": seed * 1000 + k})
+    return out, true, mig
+
+
+def ensemble_inputs(member: dict, true: np.ndarray, mig: np.ndarray):
+    """Padded true and migration velocities of one ensemble member (the realization
+    perturbs the migration model)."""
+    p, o = member["params"], member["offset"]
+    g = synth.grf_coarse((p.nx, p.nz), p.dx, 200.0, member["seed"])
+    vmig = (mig[o:o + p.nx].astype(np.float64) * np.exp(0.03 * g)).astype(np.float32)
+    return extend(p, np.ascontiguousarray(true[o:o + p.nx])), extend(p, vmig)
+
+
+SERVING_GRIDS = ((400, 200), (1200, 400), (2000, 600), (3400, 700))
+
+
+def serving_template(k: int, nt: int = 7500) -> tuple:
+    """Grid template k of the serving trace: (params with nt, true model, migration model).
+    The two smaller grids use the layered model at 10 m (dt 1 ms, CPML 40, 15 Hz), the two
+    larger the faulted model at 5 m (dt 0.4 ms, CPML 50, 20 Hz); one receiver per column,
+    shot at the surface mid-line."""
+    nx, nz = SERVING_GRIDS[k]
+    if k < 2:
+        p = params_small(nx=nx, nz=nz, shot_x=nx // 2, rec_count=nx, nt=nt)
+        true, mig = synth.layered_model(nx, nz, p.dx, 100 + k), None
+        mig = synth.smooth(true, 80.0, p.dx)
+    else:
+        p = params_large(nx=nx, nz=nz, shot_x=nx // 2, rec_count=nx, nt=nt)
+        true = synth.faulted_model(nx, nz, p.dx, 100 + k)
+        mig = synth.smooth(true, 40.0, p.dx)
+    return p, true, mig
+
+
+def serving_trace(n: int, seed: int = 23):
+    """Requests of the serving trace: grid template uniform over SERVING_GRIDS, nt uniform
+    in [2000, 7500], FP32 or BF16 ring storage, own realization seed."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        reqs.append({"grid": int(rng.integers(0, len(SERVING_GRIDS))),
+                     "nt": int(rng.integers(100, 376)) * 20,    # 2000..7500, whole slices
+                     "precision": int(rng.integers(0, 2)),
+                     "seed": seed * 100000 + i})
+    return reqs

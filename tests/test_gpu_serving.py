@@ -26,8 +26,8 @@ def _mix(eng, d):
              _case(eng, d, "quirks", storage=0),
              _case(eng, d, "uneven", storage=0, precision=1),
              _case(eng, d, "uneven", storage=1, precision=2)]
-    cases.append(_shorter(eng, cases[0], cases[0][0].nt - 37))
-    cases.append(_shorter(eng, cases[1], cases[1][0].nt // 2 + 3))
+    cases.append(_shorter(eng, cases[0], cases[0][0].nt - 60))
+    cases.append(_shorter(eng, cases[1], cases[1][0].nt - 80))
     return cases
 
 
@@ -54,7 +54,8 @@ def test_server_single_request_equals_migrate_shot(engine, name, storage):
 
 def test_server_mixed_batch_equals_each_alone(engine):
     d = load()
-    cases = [c for c in _mix(engine, d) if _valid(engine, c[0])]
+    cases = _mix(engine, d)
+    assert all(_valid(engine, c[0]) for c in cases)
     solo = [engine.migrate_shot(*c) for c in cases]
     # fewer slots than requests: members finish and new ones are admitted mid-run;
     # steps_per_launch not dividing any nt: members finish inside a graph replay
