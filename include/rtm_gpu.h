@@ -15,6 +15,8 @@
 #ifndef RTM_GPU_H
 #define RTM_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -237,6 +239,50 @@ int rtm_server_stats(const rtm_server *server, long long *cell_updates, double *
 int rtm_migrate_shot_static(const rtm_params *p, const void *d_velocity, const void *d_wavelet,
                             const void *d_seismogram, void *d_image, void *d_self_image,
                             void *stream);
+
+/* ---- seismogram decode (host) ---------------------------------------------------------------
+ * ZFP 0.5.5 fixed-accuracy stream of a 2-D float field without header, as
+ * SRC/compression_tools.c:78-135 (zfp2d_lossyDecompression) reads it: field nx (fastest) x ny
+ * over `out` (the reference passes nx = numberOfReceivers, ny = numberOfTimeStep over the flat
+ * [irec][t] seismogram), tolerance as given to zfp_stream_set_accuracy (0: lossless bound).
+ * Bit-identical to the ZFP library's decode.  RTM_ERR_DECODE if the stream ends early. */
+int rtm_zfp_decode_float2d(const void *stream, size_t bytes, double tolerance, int nx, int ny,
+                           float *out);
+/* The same from a file (the whole file is the stream).  RTM_ERR_IO if it cannot be read. */
+int rtm_zfp_decode_file(const char *path, float *array, int nx, int ny, float tolerance);
+/* The encoder side (zfp2d_lossyCompression, compression_tools.c:10-71: the seismogram
+ * generator's output): the stream zfp_compress writes for the same field and tolerance,
+ * byte for byte, flushed to whole 64-bit words.  *bytes = stream length; RTM_ERR_INVALID if
+ * `capacity` is too small (rtm_zfp_encode_bound is always enough). */
+size_t rtm_zfp_encode_bound(int nx, int ny);
+int rtm_zfp_encode_float2d(const float *in, int nx, int ny, double tolerance, void *out,
+                           size_t capacity, size_t *bytes);
+
+/* ---- the migration driver (SRC/rtm_iso2d.c:15-177, rtm_routine) ----------------------------
+ * File contracts of SRC/fixed_parameters.h: printf patterns with one %d (velocity, stacked,
+ * laplacian: the simulation id; seismogram: the shot id, 1-based).  Velocity: raw float32
+ * Nx*Nz, [x][z]; wavelet: raw float32, n_wavelet samples; seismogram: ZFP stream (above) of
+ * rec_count x nt; outputs: raw float32 Nx*Nz [x][z] -- the stacked image and its 8th-order
+ * Laplacian (laplacian_filter2D).  Shots: x = first_shot + (id - 1) * shot_spacing,
+ * z = shot_depth, id = 1..n_shots (rtm_iso2d.c:81-83); p->shot_x / shot_z are ignored. */
+typedef struct rtm_survey {
+    const char *velocity_file;      /* velocityFile */
+    const char *wavelet_file;       /* waveletFile */
+    const char *seismogram_file;    /* seismogramFile */
+    const char *stacked_file;       /* stackedFile */
+    const char *laplacian_file;     /* stackedLaplacianFile */
+    int first_shot;                 /* firstLocationShot */
+    int shot_depth;                 /* depthShot */
+    int shot_spacing;               /* spacingShot */
+    int n_shots;                    /* numberOfShots */
+    float zfp_tolerance;            /* zfp_tolerance */
+} rtm_survey;
+/* Runs the whole migration of one simulation: per shot a forward propagation on the GPU
+ * with the shot's seismogram decoded on the host meanwhile, then the adjoint propagation;
+ * the per-shot images stay in memory (no TEMPORARY_FILES) and are stacked in shot order in
+ * float32 as the reference stacks them; both output files are written.  RTM_ERR_IO when an
+ * input cannot be read or an output written (the reference exits instead). */
+int rtm_routine_run(const rtm_params *p, const rtm_survey *survey, int simulation_id);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "librtmgpu.so")
+DROPIN_LIB = os.path.join(OUT, "librtm_dropin.so")     # the reference's entry-point names
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
@@ -25,7 +26,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + IN
 CC_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=gnu99", "-I" + INCLUDE]
 
 CU_SOURCES = ["rtm_kernels.cu", "rtm_engine.cu"]
-C_SOURCES = ["rtm_host.c"]
+C_SOURCES = ["rtm_host.c", "rtm_zfp.c", "rtm_driver.c"]
+DROPIN_SOURCES = ["rtm_dropin.c"]
 
 
 def nvcc() -> str:
@@ -53,7 +55,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     os.makedirs(OUT, exist_ok=True)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + \
            [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
-    if not force and _newer(LIB, deps):
+    if not force and _newer(LIB, deps) and _newer(DROPIN_LIB, deps):
         return LIB
     jobs = []
     for src in CU_SOURCES:
@@ -73,6 +75,15 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     tmp = LIB + ".tmp"
     _run([nvcc()] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lcudart"])
     os.replace(tmp, LIB)
+    # the drop-in library: the reference's names over librtmgpu (found next to it)
+    objs = []
+    for src in DROPIN_SOURCES:
+        obj = os.path.join(OUT, src + ".o")
+        _run(["gcc"] + CC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+        objs.append(obj)
+    tmp = DROPIN_LIB + ".tmp"
+    _run(["gcc", "-shared", "-o", tmp] + objs + ["-L" + OUT, "-lrtmgpu", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, DROPIN_LIB)
     return LIB
 
 

@@ -82,6 +82,26 @@ class RtmParams(C.Structure):
         return "RtmParams(%s)" % ", ".join("%s=%r" % kv for kv in self.as_dict().items())
 
 
+class RtmSurvey(C.Structure):
+    """rtm_survey: file patterns and shot layout of the migration driver (rtm_iso2d.c)."""
+    _fields_ = [("velocity_file", C.c_char_p), ("wavelet_file", C.c_char_p),
+                ("seismogram_file", C.c_char_p), ("stacked_file", C.c_char_p),
+                ("laplacian_file", C.c_char_p), ("first_shot", C.c_int), ("shot_depth", C.c_int),
+                ("shot_spacing", C.c_int), ("n_shots", C.c_int), ("zfp_tolerance", C.c_float)]
+
+    @classmethod
+    def make(cls, velocity_file, wavelet_file, seismogram_file, stacked_file, laplacian_file,
+             first_shot, shot_depth, shot_spacing=0, n_shots=1, zfp_tolerance=0.0) -> "RtmSurvey":
+        s = cls()
+        s._keep = [x.encode() for x in (velocity_file, wavelet_file, seismogram_file, stacked_file,
+                                         laplacian_file)]
+        (s.velocity_file, s.wavelet_file, s.seismogram_file, s.stacked_file,
+         s.laplacian_file) = s._keep
+        s.first_shot, s.shot_depth, s.shot_spacing = first_shot, shot_depth, shot_spacing
+        s.n_shots, s.zfp_tolerance = n_shots, zfp_tolerance
+        return s
+
+
 class RtmError(RuntimeError):
     def __init__(self, status: int, detail: str):
         super().__init__("%s: %s" % (status_string(status), detail))
@@ -145,6 +165,12 @@ def _declare(L):
         "rtm_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "rtm_migrate_shot_static": (C.c_int, [P, vp, vp, vp, vp, vp, vp]),
+        "rtm_zfp_decode_float2d": (C.c_int, [vp, C.c_size_t, C.c_double, C.c_int, C.c_int, fp]),
+        "rtm_zfp_decode_file": (C.c_int, [C.c_char_p, fp, C.c_int, C.c_int, C.c_float]),
+        "rtm_zfp_encode_bound": (C.c_size_t, [C.c_int, C.c_int]),
+        "rtm_zfp_encode_float2d": (C.c_int, [fp, C.c_int, C.c_int, C.c_double, vp, C.c_size_t,
+                                             C.POINTER(C.c_size_t)]),
+        "rtm_routine_run": (C.c_int, [P, C.POINTER(RtmSurvey), C.c_int]),
         "rtm_plan_profile": (C.c_int, [vp, C.c_int]),
         "rtm_plan_profile_read": (C.c_int, [vp, C.POINTER(C.c_double), ip, C.POINTER(C.c_double), ip]),
     }
@@ -165,7 +191,9 @@ def exported_symbols():
             "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_launch_count",
             "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
             "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_step",
-            "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static"]
+            "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static",
+            "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
+            "rtm_zfp_encode_float2d", "rtm_routine_run"]
 
 
 def status_string(st: int) -> str:
@@ -283,6 +311,40 @@ def laplacian_filter2D(p: RtmParams, image) -> np.ndarray:
     out = np.zeros((p.nx, p.nz), np.float32)
     _check(lib().rtm_laplacian_filter2D(C.byref(p), _fp(out), _fp(_f32(image))))
     return out
+
+
+def zfp_decode(stream: bytes, nx: int, ny: int, tolerance: float) -> np.ndarray:
+    """ZFP 0.5.5 fixed-accuracy decode of an nx (fastest) x ny float field; returned as the
+    reference's flat buffer viewed (nx, ny) -- (rec_count, nt) for a seismogram."""
+    buf = np.frombuffer(bytes(stream), np.uint8)
+    out = np.empty(nx * ny, np.float32)
+    _check(lib().rtm_zfp_decode_float2d(buf.ctypes.data_as(C.c_void_p), buf.size, float(tolerance),
+                                        nx, ny, _fp(out)))
+    return out.reshape(nx, ny)
+
+
+def zfp_encode(field: np.ndarray, tolerance: float) -> bytes:
+    """ZFP 0.5.5 fixed-accuracy stream of a (nx, ny) float field in the reference's flat
+    layout (zfp nx = field.shape[0] fastest) -- what zfp2d_lossyCompression writes."""
+    a = _f32(field)
+    nx, ny = a.shape
+    cap = lib().rtm_zfp_encode_bound(nx, ny)
+    buf = np.empty(cap, np.uint8)
+    n = C.c_size_t()
+    _check(lib().rtm_zfp_encode_float2d(_fp(a), nx, ny, float(tolerance), buf.ctypes.data_as(C.c_void_p),
+                                        cap, C.byref(n)))
+    return buf[: n.value].tobytes()
+
+
+def routine_run(p: RtmParams, survey: RtmSurvey, simulation_id: int) -> None:
+    """The migration driver of one simulation on files (rtm_iso2d.c:15-177)."""
+    _check(lib().rtm_routine_run(C.byref(p), C.byref(survey), simulation_id))
+
+
+def dropin_lib():
+    """librtm_dropin.so: the reference's entry-point names over the engine."""
+    lib()
+    return C.CDLL(_build.DROPIN_LIB)
 
 
 def release_cached() -> None:

@@ -1,0 +1,110 @@
+/*
+ * rtm_driver.c -- the migration driver of one simulation, SRC/rtm_iso2d.c:15-177
+ * (rtm_routine), over the engine's C ABI.
+ *
+ * Same inputs, outputs and arithmetic of the stack as the reference: velocity and wavelet
+ * read raw (pi_file.c:11-32), edge-replicated into the CPML (extend_matrix), per shot a
+ * forward propagation, the shot's ZFP seismogram decoded, an adjoint propagation into a
+ * zeroed image and self image; images summed over shots in float32 in shot order
+ * (rtm_iso2d.c:115-129), the stack written, its Laplacian (laplacian_filter2D) written.
+ * Differences: the per-shot images stay in host memory instead of TEMPORARY_FILES
+ * round trips (rtm_iso2d.c:95-103, 108-140), the decode runs while the GPU propagates
+ * (rtm_forward_modeling returns once the forward pass is queued), and errors are returned
+ * (RTM_ERR_IO) where the reference exits.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "rtm_gpu.h"
+
+#define RTM_PATH_LEN 4096
+
+static int read_raw(const char *path, float *dst, size_t n)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) return RTM_ERR_IO;
+    const size_t got = fread(dst, sizeof(float), n, f);
+    fclose(f);
+    return got == n ? RTM_OK : RTM_ERR_IO;
+}
+
+static int write_raw(const char *path, const float *src, size_t n)
+{
+    FILE *f = fopen(path, "wb");
+    if (!f) return RTM_ERR_IO;
+    const size_t put = fwrite(src, sizeof(float), n, f);
+    const int closed = fclose(f);
+    return (put == n && closed == 0) ? RTM_OK : RTM_ERR_IO;
+}
+
+static int format_path(char *out, const char *pattern, int id)
+{
+    if (!pattern) return RTM_ERR_INVALID;
+    const int n = snprintf(out, RTM_PATH_LEN, pattern, id);
+    return (n < 0 || n >= RTM_PATH_LEN) ? RTM_ERR_INVALID : RTM_OK;
+}
+
+int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulation_id)
+{
+    if (!params || !s || !s->velocity_file || !s->wavelet_file || !s->seismogram_file ||
+        !s->stacked_file || !s->laplacian_file || s->n_shots < 0)
+        return RTM_ERR_INVALID;
+    rtm_params p = *params;
+    p.shot_x = s->first_shot;
+    p.shot_z = s->shot_depth;
+    int st = rtm_params_check(&p);
+    if (st != RTM_OK) return st;
+
+    const size_t nimg = (size_t)p.nx * (size_t)p.nz;
+    const size_t next = (size_t)(p.th_left + p.nx + p.th_right) * (size_t)(p.th_up + p.nz + p.th_down);
+    const size_t nseis = (size_t)p.rec_count * (size_t)p.nt;
+    const size_t nwav = p.n_wavelet > 0 ? (size_t)p.n_wavelet : 1;
+    float *model = (float *)calloc(nimg, sizeof(float));
+    float *ext = (float *)calloc(next, sizeof(float));
+    float *wav = (float *)calloc(nwav, sizeof(float));
+    float *seis = (float *)calloc(nseis > 0 ? nseis : 1, sizeof(float));
+    float *img = (float *)calloc(nimg, sizeof(float));
+    float *slf = (float *)calloc(nimg, sizeof(float));
+    float *stack = (float *)calloc(nimg, sizeof(float));
+    float *lap = (float *)calloc(nimg, sizeof(float));
+    char path[RTM_PATH_LEN];
+    if (!model || !ext || !wav || !seis || !img || !slf || !stack || !lap) {
+        st = RTM_ERR_NOMEM;
+        goto done;
+    }
+    /* rtm_iso2d.c:70-75 */
+    if ((st = format_path(path, s->velocity_file, simulation_id)) != RTM_OK) goto done;
+    if ((st = read_raw(path, model, nimg)) != RTM_OK) goto done;
+    if (p.n_wavelet > 0 && (st = read_raw(s->wavelet_file, wav, (size_t)p.n_wavelet)) != RTM_OK) goto done;
+    rtm_extend_matrix(&p, ext, model);
+
+    /* rtm_iso2d.c:77-104: shots in an arithmetic progression */
+    for (int shot_id = 1; shot_id <= s->n_shots; ++shot_id) {
+        int shot[2];
+        shot[0] = s->first_shot + (shot_id - 1) * s->shot_spacing;
+        shot[1] = s->shot_depth;
+        p.shot_x = shot[0];
+        p.shot_z = shot[1];
+        if ((st = rtm_forward_modeling(&p, simulation_id, shot, ext, wav)) != RTM_OK) goto done;
+        /* the decode overlaps the queued forward propagation */
+        if ((st = format_path(path, s->seismogram_file, shot_id)) != RTM_OK) goto done;
+        if (nseis > 0 && (st = rtm_zfp_decode_file(path, seis, p.rec_count, p.nt, s->zfp_tolerance)) != RTM_OK)
+            goto done;
+        memset(img, 0, nimg * sizeof(float));
+        memset(slf, 0, nimg * sizeof(float));
+        if ((st = rtm_adjoint_modeling(&p, simulation_id, shot, ext, wav, seis, img, slf)) != RTM_OK) goto done;
+        /* rtm_iso2d.c:121-126: float sum in shot order */
+        for (size_t i = 0; i < nimg; ++i) stack[i] = stack[i] + img[i];
+    }
+    /* rtm_iso2d.c:148-164 (the normalisation at :152 is commented out in the reference) */
+    if ((st = format_path(path, s->stacked_file, simulation_id)) != RTM_OK) goto done;
+    if ((st = write_raw(path, stack, nimg)) != RTM_OK) goto done;
+    if ((st = rtm_laplacian_filter2D(&p, lap, stack)) != RTM_OK) goto done;
+    if ((st = format_path(path, s->laplacian_file, simulation_id)) != RTM_OK) goto done;
+    st = write_raw(path, lap, nimg);
+done:
+    free(model); free(ext); free(wav); free(seis);
+    free(img); free(slf); free(stack); free(lap);
+    return st;
+}

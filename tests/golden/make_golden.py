@@ -6,8 +6,9 @@ on small seeded inputs:
 
   extend_matrix, attenuation_profile_cpml, iso_acoustic_wave_equation,
   aiso_attenuation_cpml, laplacian_filter2D, isotropicAcousticModeling (its snapshot
-  file), isotropicAcousticModeling + adjointModeling (image, self image), and the ZFP
-  round trip through zfp2d_lossyCompression / zfp2d_lossyDecompression.
+  file), isotropicAcousticModeling + adjointModeling (image, self image), the ZFP
+  round trip through zfp2d_lossyCompression / zfp2d_lossyDecompression, and the whole
+  driver rtm_routine on files (two shots, ZFP seismograms, stacked image and Laplacian).
 
 Needs the reference tree (default /root/reference, or RTM_REFERENCE_ROOT).  Run:
     python tests/golden/make_golden.py
@@ -118,6 +119,48 @@ def main():
         out["zfp/" + tag + "/stream"] = np.frombuffer(blob, np.uint8)
         out["zfp/" + tag + "/decoded"] = dec.reshape(seis.shape)
     out["zfp/input"] = seis
+    # partial edge blocks in both directions (7 receivers x 158 samples)
+    part = np.ascontiguousarray(out["quirks/seis"][:, :158])
+    blob = ref.zfp_compress(part, part.shape[0], part.shape[1], 1e-4)
+    with tempfile.NamedTemporaryFile(suffix=".zfp", delete=False) as f:
+        f.write(blob)
+        path = f.name
+    try:
+        dec = ref.zfp_decompress(path, part.shape[0], part.shape[1], 1e-4)
+    finally:
+        os.unlink(path)
+    out["zfp/partial/input"] = part
+    out["zfp/partial/stream"] = np.frombuffer(blob, np.uint8)
+    out["zfp/partial/decoded"] = dec.reshape(part.shape)
+
+    # the whole driver: rtm_routine(sim_id) on files (2 shots, ZFP tol 1e-4 seismograms)
+    p = dict(CASES["uneven"])
+    sim_id, n_shots, first, spacing, tol = 3, 2, 22, 16, 1e-4
+    model = out["uneven/model"]
+    wav = out["uneven/wavelet"]
+    ext_true = ref.extend_matrix(p, model * np.float32(1.04))
+    with tempfile.TemporaryDirectory() as tmp:
+        for d in ("INPUTS", "OUTPUTS", "TEMPORARY_FILES"):
+            os.makedirs(os.path.join(tmp, d))
+        model.astype(np.float32).tofile(os.path.join(tmp, "INPUTS", "vp_%05d.bin" % sim_id))
+        wav.astype(np.float32).tofile(os.path.join(tmp, "INPUTS", "wavelet.bin"))
+        for shot_id in range(1, n_shots + 1):
+            q = dict(p, shot_x=first + (shot_id - 1) * spacing)
+            seis = orc.model_seismogram(q, ext_true, wav)
+            blob = ref.zfp_compress(seis, seis.shape[0], seis.shape[1], tol)
+            with open(os.path.join(tmp, "INPUTS", "seismogram_%05d.zfp" % shot_id), "wb") as f:
+                f.write(blob)
+            out["routine/seis_%d" % shot_id] = np.frombuffer(blob, np.uint8)
+        ref.configure(dict(p, shot_x=first), n_shots=n_shots, spacing_shot=spacing, zfp_tolerance=tol)
+        ref.set_paths("./INPUTS/vp_%05d.bin", "./INPUTS/wavelet.bin", "./INPUTS/seismogram_%05d.zfp",
+                      "./OUTPUTS/stackedBrute_%05d.bin", "./OUTPUTS/stackedLaplacian_%05d.bin")
+        ref.rtm_routine(tmp, sim_id)
+        out["routine/stacked"] = np.fromfile(os.path.join(tmp, "OUTPUTS", "stackedBrute_%05d.bin" % sim_id),
+                                             np.float32).reshape(p["nx"], p["nz"])
+        out["routine/laplacian"] = np.fromfile(
+            os.path.join(tmp, "OUTPUTS", "stackedLaplacian_%05d.bin" % sim_id), np.float32).reshape(p["nx"], p["nz"])
+    out["routine/survey"] = np.array([sim_id, n_shots, first, spacing, p["shot_z"]], np.int32)
+    out["routine/tol"] = np.array([tol], np.float32)
 
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

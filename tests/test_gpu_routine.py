@@ -1,0 +1,68 @@
+"""The migration driver on files (rtm_routine, SRC/rtm_iso2d.c:15-177) against the
+reference's own rtm_routine run on the same files (tests/golden/make_golden.py): two shots,
+ZFP tol 1e-4 seismograms, stacked image and its Laplacian.  Run through the engine's C
+entry point and through the reference-named drop-in library."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from golden_util import case_params, load, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(engine, tmp_path):
+    d = load()
+    sim_id, n_shots, first, spacing, depth = (int(v) for v in d["routine/survey"])
+    tol = float(d["routine/tol"][0])
+    for sub in ("INPUTS", "OUTPUTS"):
+        (tmp_path / sub).mkdir()
+    d["uneven/model"].astype(np.float32).tofile(tmp_path / "INPUTS" / ("vp_%05d.bin" % sim_id))
+    d["uneven/wavelet"].astype(np.float32).tofile(tmp_path / "INPUTS" / "wavelet.bin")
+    for k in range(1, n_shots + 1):
+        (tmp_path / "INPUTS" / ("seismogram_%05d.zfp" % k)).write_bytes(d["routine/seis_%d" % k].tobytes())
+    p = engine.RtmParams.make(**case_params(d, "uneven"))
+    s = engine.RtmSurvey.make(str(tmp_path / "INPUTS" / "vp_%05d.bin"), str(tmp_path / "INPUTS" / "wavelet.bin"),
+                              str(tmp_path / "INPUTS" / "seismogram_%05d.zfp"),
+                              str(tmp_path / "OUTPUTS" / "stackedBrute_%05d.bin"),
+                              str(tmp_path / "OUTPUTS" / "stackedLaplacian_%05d.bin"),
+                              first_shot=first, shot_depth=depth, shot_spacing=spacing, n_shots=n_shots,
+                              zfp_tolerance=tol)
+    return d, p, s, sim_id
+
+
+def _outputs(d, tmp_path, sim_id):
+    p = case_params(d, "uneven")
+    st = np.fromfile(tmp_path / "OUTPUTS" / ("stackedBrute_%05d.bin" % sim_id), np.float32)
+    lp = np.fromfile(tmp_path / "OUTPUTS" / ("stackedLaplacian_%05d.bin" % sim_id), np.float32)
+    return st.reshape(p["nx"], p["nz"]), lp.reshape(p["nx"], p["nz"])
+
+
+@pytest.mark.parametrize("storage", (0, 1))
+def test_routine_matches_reference(engine, tmp_path, storage):
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    engine.routine_run(p.replace(storage=storage), s, sim_id)
+    st, lp = _outputs(d, tmp_path, sim_id)
+    assert rel_l2(st, d["routine/stacked"]) <= 1e-4
+    assert rel_l2(lp, d["routine/laplacian"]) <= 1e-4
+
+
+def test_dropin_rtm_routine_matches_reference(engine, tmp_path):
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    L = engine.dropin_lib()
+    L.rtm_dropin_configure.argtypes = [C.POINTER(engine.RtmParams), C.POINTER(engine.RtmSurvey)]
+    assert L.rtm_dropin_configure(C.byref(p), C.byref(s)) == 0
+    L.rtm_routine(C.c_int(sim_id))
+    st, lp = _outputs(d, tmp_path, sim_id)
+    assert rel_l2(st, d["routine/stacked"]) <= 1e-4
+    assert rel_l2(lp, d["routine/laplacian"]) <= 1e-4
+
+
+def test_routine_missing_input_is_an_io_error(engine, tmp_path):
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    os.unlink(tmp_path / "INPUTS" / "seismogram_00002.zfp")
+    with pytest.raises(engine.RtmError) as e:
+        engine.routine_run(p, s, sim_id)
+    assert e.value.status == 6

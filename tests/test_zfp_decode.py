@@ -1,0 +1,100 @@
+"""The engine's ZFP 0.5.5 fixed-accuracy decoder (host) against the reference's own ZFP
+build: the golden streams were written by zfp2d_lossyCompression and decoded by
+zfp2d_lossyDecompression (tests/golden/make_golden.py); the decode must be bit-identical."""
+import numpy as np
+import pytest
+
+from golden_util import load
+
+
+@pytest.mark.parametrize("tag,tol", (("tol1e-4", 1e-4), ("tol0", 0.0)))
+def test_decode_bit_identical_to_reference(engine, tag, tol):
+    d = load()
+    stream = d["zfp/%s/stream" % tag].tobytes()
+    ref = d["zfp/%s/decoded" % tag]
+    nrec, nt = ref.shape
+    # the reference passes dimension1 = numberOfReceivers (zfp nx), dimension2 = nt (zfp ny)
+    out = engine.zfp_decode(stream, nrec, nt, np.float32(tol))
+    assert out.dtype == np.float32 and out.shape == ref.shape
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+    if tol > 0:
+        err = np.abs(out - d["zfp/input"]).max()
+        assert 0 < err <= tol
+
+
+def test_decode_routine_streams_match_tolerance(engine):
+    """The driver fixture's seismogram streams decode to fields within the tolerance of each
+    other's shot geometry: a sanity check that every stream decodes to its full length."""
+    d = load()
+    nrec, nt = int(d["uneven/params"][12]), int(d["uneven/params"][6])
+    for k in (1, 2):
+        out = engine.zfp_decode(d["routine/seis_%d" % k].tobytes(), nrec, nt, d["routine/tol"][0])
+        assert np.isfinite(out).all() and np.abs(out).max() > 0
+
+
+def test_truncated_stream_is_an_error(engine):
+    d = load()
+    stream = d["zfp/tol0/stream"].tobytes()
+    nrec, nt = d["zfp/tol0/decoded"].shape
+    with pytest.raises(engine.RtmError) as e:
+        engine.zfp_decode(stream[: len(stream) // 2], nrec, nt, 0.0)
+    assert e.value.status == 7          # RTM_ERR_DECODE
+
+
+def test_file_decode_and_missing_file(engine, tmp_path):
+    import ctypes as C
+    d = load()
+    path = tmp_path / "s.zfp"
+    path.write_bytes(d["zfp/tol1e-4/stream"].tobytes())
+    ref = d["zfp/tol1e-4/decoded"]
+    out = np.empty(ref.size, np.float32)
+    L = engine.lib()
+    st = L.rtm_zfp_decode_file(str(path).encode(), out.ctypes.data_as(C.POINTER(C.c_float)),
+                               ref.shape[0], ref.shape[1], C.c_float(1e-4))
+    assert st == 0 and np.array_equal(out.reshape(ref.shape), ref)
+    st = L.rtm_zfp_decode_file(str(tmp_path / "missing.zfp").encode(),
+                               out.ctypes.data_as(C.POINTER(C.c_float)), ref.shape[0], ref.shape[1],
+                               C.c_float(1e-4))
+    assert st == 6                      # RTM_ERR_IO
+
+
+def test_dropin_library_exports_reference_names(engine):
+    import os
+    import re
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "rtm_dropin.h")).read()
+    body = hdr.split("#ifdef FIXED_PARAMETERS_H")[0]
+    names = set(re.findall(r"^(?:void|int)\s+(\w+)\s*\(", body, re.M))
+    assert {"rtm_routine", "isotropicAcousticModeling", "adjointModeling", "zfp2d_lossyDecompression",
+            "iso_acoustic_wave_equation", "aiso_attenuation_cpml", "laplacian_filter2D"} <= names
+    L = engine.dropin_lib()
+    for n in sorted(names):
+        assert hasattr(L, n), n
+
+
+@pytest.mark.parametrize("tag,tol", (("tol1e-4", 1e-4), ("tol0", 0.0)))
+def test_encode_byte_identical_to_reference(engine, tag, tol):
+    d = load()
+    stream = engine.zfp_encode(d["zfp/input"], np.float32(tol))
+    assert stream == d["zfp/%s/stream" % tag].tobytes()
+
+
+def test_partial_blocks_encode_and_decode(engine):
+    """7 x 158 field: edge blocks partial in both directions (ZFP's padding rule)."""
+    d = load()
+    inp, ref_stream, ref_dec = d["zfp/partial/input"], d["zfp/partial/stream"], d["zfp/partial/decoded"]
+    assert engine.zfp_encode(inp, np.float32(1e-4)) == ref_stream.tobytes()
+    out = engine.zfp_decode(ref_stream.tobytes(), inp.shape[0], inp.shape[1], np.float32(1e-4))
+    assert np.array_equal(out.view(np.uint32), ref_dec.view(np.uint32))
+
+
+def test_encode_decode_round_trip_bound(engine):
+    rng = np.random.default_rng(3)
+    # magnitudes below 2, so float32 resolves every tolerance tried
+    f = (rng.standard_normal((33, 45)) * np.exp(rng.uniform(-20, -1.5, (33, 45)))).astype(np.float32)
+    f[3:9, 4:12] = 0.0
+    for tol in (1e-2, 1e-4, 1e-6):
+        out = engine.zfp_decode(engine.zfp_encode(f, tol), 33, 45, tol)
+        assert np.abs(out - f).max() <= tol
+    lossless = engine.zfp_decode(engine.zfp_encode(f, 0.0), 33, 45, 0.0)
+    assert np.abs(lossless - f).max() <= 1e-6 * np.abs(f).max()
