@@ -31,83 +31,420 @@ __host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
     n[3] = (g.dimx - 8) * ((g.dimz - 4 - q0 + 3) / 4);
 }
 
-// Step arguments of member M at (pass, t), as run_forward / run_adjoint set them.
+// Slot k of a member's source-wavefield store and its scales (16-bit storage).
 template <typename T>
-__device__ __forceinline__ void member_args(const BMember<T> &M, int pass, int t, StepArgs<T> &a,
-                                            int &cur, int &sc, int &sp)
+__device__ __forceinline__ void *member_slot(const BMember<T> &M, int k)
+{
+    const size_t se = M.store_prec == 0 ? sizeof(T) : 2;
+    return static_cast<unsigned char *>(M.store) + (size_t)k * M.slot_elems * se;
+}
+template <typename T>
+__device__ __forceinline__ float *member_scales(const BMember<T> &M, int k)
+{
+    return M.scales ? M.scales + (size_t)k * M.scales_per_slot : nullptr;
+}
+
+// ctrl of the reference's imaging loop at tau (backward_modeling.c:267): it starts at
+// nt/slices - 1 at the first tau % slices == 0 and counts down, so it lags tau/slices by one
+// when slices does not divide nt.
+__host__ __device__ __forceinline__ int image_ctrl(const Geom &g, int tau)
+{
+    return g.nt / g.slices - 1 - ((g.nt - 1) / g.slices - tau / g.slices);
+}
+
+// Arguments of member M's tiles of role `role` at step t of its pass, and the tensor maps
+// they load (mu: field with halo, mp: previous field; u maps for FWD/SRC, r maps for RCV).
+// Mirrors the single-migration drivers run_forward / run_adjoint (forward_modeling.c:98-128,
+// backward_modeling.c:268-297), with the imaging moved one step later (rtm_march.cuh).
+template <typename T>
+__device__ __forceinline__ void margs(const BMember<T> &M, int t, int role, MArgs<T> &a, int &mu, int &mp)
 {
     const Geom &g = M.g;
     a.g = g;
-    a.h1 = M.h1; a.h2 = M.h2; a.h3 = M.h3;
-    a.psi_l = M.psi[0]; a.psi_r = M.psi[1]; a.psi_t = M.psi[2]; a.psi_b = M.psi[3];
-    a.xi_l = M.xi[0]; a.xi_r = M.xi[1]; a.xi_t = M.xi[2]; a.xi_b = M.xi[3];
-    a.a_l = M.prof[0]; a.b_l = M.prof[1]; a.a_r = M.prof[2]; a.b_r = M.prof[3];
-    a.a_t = M.prof[4]; a.b_t = M.prof[5]; a.a_b = M.prof[6]; a.b_b = M.prof[7];
-    a.rec_last = M.rec_last; a.rec_first = M.rec_first; a.rec_cnt = M.rec_cnt;
-    a.store_prec = M.store_prec;
-    a.img = M.img; a.slf = M.slf;
-    a.status = M.status;
     a.wavelet = M.wav;
-    a.rec_out = nullptr;
-    a.t = t;
-    a.s_next = nullptr; a.s_snap = nullptr; a.s_fixed = nullptr;
-    a.store = nullptr; a.store_scale = nullptr;
+    a.rec_last = M.rec_last; a.rec_first = M.rec_first; a.rec_cnt = M.rec_cnt;
     a.seis_row = nullptr;
+    a.rec_out = nullptr;
+    a.store = nullptr; a.store_scale = nullptr;
+    a.s_img = nullptr;
+    a.img = M.img; a.slf = M.slf;
+    a.t = t;
+    a.tsrc = 0;
+    a.store_prec = M.store_prec;
     const bool ring = M.storage == 1;
-    const size_t se = M.store_prec == 0 ? sizeof(T) : 2;
-    auto slot = [&](int k) { return static_cast<void *>(static_cast<unsigned char *>(M.store) + (size_t)k * M.slot_elems * se); };
-    auto scl = [&](int k) { return M.scales ? M.scales + (size_t)k * g.tiles : (float *)nullptr; };
-    int f = (t == 0) ? F_STRIPS_FRESH : 0;   // psi/xi of this pass start from zero
-    cur = t & 1;
-    sc = sp = 0;
-    if (pass == 1) {                      // forward: forward_modeling.c:98-128
-        a.u_next = M.u[1 - cur];
+    const int cur = t & 1;
+    const int ua = g.nt & 1, ub = 1 - ua;          // u buffers holding u_nt, u_{nt-1}
+    int f = 0;
+    if (role == ROLE_FWD) {
+        mu = cur; mp = 1 - cur;
+        a.out = M.u[1 - cur];
         if (t < g.nwav) f |= F_SRC;
-        if (ring) {
-            f |= F_RING_SAVE;
-            a.store = slot(t + 1);
-            a.store_scale = scl(t + 1);
-        } else if (t % g.slices == 0) {
+        if (M.rec_out) { f |= F_RECORD; a.rec_out = M.rec_out; }
+        if (!ring && t % g.slices == 0) {
             f |= F_SNAP_SAVE;
-            a.store = slot(t / g.slices);
-            a.store_scale = scl(t / g.slices);
+            a.store = member_slot(M, t / g.slices);
+            a.store_scale = member_scales(M, t / g.slices);
         }
-    } else {                              // backward: backward_modeling.c:268-297
-        const int tau = g.nt - t - 1;
-        a.u_next = M.r[1 - cur];
-        if (g.nrec > 0) {
+    } else if (role == ROLE_RCV) {
+        mu = cur; mp = 1 - cur;
+        a.out = M.r[1 - cur];
+        if (t == g.nt) f |= F_NO_STEP;             // image-only step after the last one
+        else if (g.nrec > 0) {
             f |= F_OVERWRITE;
-            a.seis_row = M.seis_t + (size_t)tau * g.nrec;
+            a.seis_row = M.seis_t + (size_t)(g.nt - 1 - t) * g.nrec;
         }
-        const int ua = g.nt & 1, ub = 1 - ua;     // buffers holding u_nt, u_{nt-1}
-        const bool recon = ring && t >= 2;
-        if (recon) {
-            f |= F_RECON;
-            if (tau + 2 < g.nwav) f |= F_RECON_SRC;
-            sc = ((t - 2) & 1) ? ua : ub;
-            sp = 1 - sc;
-            a.s_next = M.u[sp];
-            a.store = slot(tau + 1);
-            a.store_scale = scl(tau + 1);
+        if (t >= 1) {                              // image of step t-1
+            const int taup = g.nt - t;
+            const int ctrl = image_ctrl(g, taup);
+            if (taup % g.slices == 0 && ctrl >= 0) {
+                f |= F_IMAGE;
+                if (ring) {
+                    a.s_img = M.u[((t - 1) & 1) ? ub : ua];   // S(j) lives in u[ua] for even j
+                } else {
+                    f |= F_IMAGE_SNAP;
+                    a.store = member_slot(M, ctrl);
+                    a.store_scale = member_scales(M, ctrl);
+                }
+            }
         }
-        // imaging at tau % slices == 0 with the reference's snapshot counter
-        // (backward_modeling.c:267): ctrl starts at nt/slices - 1 at the first such tau and
-        // counts down, so it lags tau/slices by one when slices does not divide nt
-        const int ctrl = g.nt / g.slices - 1 - ((g.nt - 1) / g.slices - tau / g.slices);
-        if (tau % g.slices == 0 && ctrl >= 0) {
-            f |= F_IMAGE;
-            if (!ring) {
-                f |= F_IMAGE_SNAP;
-                a.s_snap = static_cast<const T *>(slot(ctrl));
-                a.store = slot(ctrl);
-                a.store_scale = scl(ctrl);
-            } else if (!recon) {
-                f |= F_IMAGE_FIXED;
-                a.s_fixed = t == 0 ? M.u[ua] : M.u[ub];
+    } else {                                       // ROLE_SRC, 2 <= t < nt
+        const int tau = g.nt - 1 - t;
+        const int sc = ((t - 2) & 1) ? ua : ub, sp = 1 - sc;
+        mu = sc; mp = sp;
+        a.out = M.u[sp];
+        if (tau + 2 < g.nwav) { f |= F_RECON_SRC; a.tsrc = tau + 2; }
+    }
+    a.flags = f;
+}
+
+// ---- strip kernel (k_bstrip) ------------------------------------------------------------
+// For one quad of a strip: xi_n = b xi_{n-1} + a (D2(u_n) / dx^2 + D1(psi_n) / dx) and the
+// correction coef dx^2 (D1(psi_n)/dx + xi_n) that the reference adds to u_{n+1}
+// (absorbingBoundaryCondition.c:191-217 left, 237-263 top, 283-310 right, 330-357 bottom);
+// same arithmetic as cpml_x_quad / cpml_z_quad (rtm_step.cuh).  c4 gets the correction.
+template <typename T>
+__device__ __forceinline__ void strip_x_quad(const T *psi, T *xi, size_t P, T ab, T bb, const T (&W)[9][4],
+                                             const T (&cf)[4], int zq, int zlo, int zhi, T h1, T h2, T h3,
+                                             bool fresh, T (&c4)[4])
+{
+    T acc[4];
+    {
+        const T bk[4] = {(T)RTM_B4, (T)RTM_B3, (T)RTM_B2, (T)RTM_B1};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            T mk[4], pk[4];
+            ld4(psi - (ptrdiff_t)(4 - k) * (ptrdiff_t)P, mk);
+            ld4(psi + (ptrdiff_t)(4 - k) * (ptrdiff_t)P, pk);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const T term = bk[k] * (pk[j] - mk[j]);
+                acc[j] = k == 0 ? term : acc[j] + term;
             }
         }
     }
-    a.flags = f;
+    T x4[4];
+    if (fresh) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
+    } else {
+        ld4(xi, x4);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = zq + j;
+        c4[j] = (T)0;
+        if (z >= zlo && z < zhi) {
+            const T dp = acc[j] * h1;
+            const T xn = bb * x4[j] + ab * (d2x_w<T>(W, j) * h3 + dp);
+            x4[j] = xn;
+            c4[j] = (cf[j] * h2) * (dp + xn);
+        }
+    }
+    st4(xi, x4);
+}
+
+template <typename T>
+__device__ __forceinline__ void strip_z_quad(const T *psi, T *xi, const float *ab, const float *bb,
+                                             const T (&zz)[12], const T (&cf)[4], int zq, int zlo, int zhi,
+                                             T h1, T h2, T h3, bool fresh, T (&c4)[4])
+{
+    T q[12];
+    {
+        T a0[4], a1[4], a2[4];
+        ld4(psi - 4, a0);
+        ld4(psi, a1);
+        ld4(psi + 4, a2);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { q[j] = a0[j]; q[4 + j] = a1[j]; q[8 + j] = a2[j]; }
+    }
+    T x4[4];
+    if (fresh) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
+    } else {
+        ld4(xi, x4);
+    }
+    const float4 av = *reinterpret_cast<const float4 *>(ab);
+    const float4 bv = *reinterpret_cast<const float4 *>(bb);
+    const float aa[4] = {av.x, av.y, av.z, av.w}, bbv[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = zq + j;
+        c4[j] = (T)0;
+        if (z >= zlo && z < zhi) {
+            const T dp = dpsi_z<T>(q, j) * h1;
+            const T xn = (T)bbv[j] * x4[j] + (T)aa[j] * (d2z_q<T>(zz, j) * h3 + dp);
+            x4[j] = xn;
+            c4[j] = (cf[j] * h2) * (dp + xn);
+        }
+    }
+    st4(xi, x4);
+}
+
+// Strip quads of one member: every strip column x in [4, thl-4) or [dimx-thr+4, dimx-4)
+// with all its z quads in [4, dimz-4) (nA items), then every column x in [0, dimx) with its
+// top quads (z in [4, thu-4)) and bottom quads (z in [dimz-thd+4, dimz-4)) -- items of strip
+// columns (already covered) or bottom quads outside [4, dimx-4) are skipped (nB items).
+struct CorrShape {
+    int nql, nA, ntq, q0, nbq, nB;
+};
+__host__ __device__ __forceinline__ CorrShape corr_shape(const Geom &g)
+{
+    CorrShape c;
+    c.nql = (g.dimz - 8 + 3) / 4;
+    c.nA = (g.thl - 8 + g.thr - 8) * c.nql;
+    c.ntq = (g.thu - 8 + 3) / 4;
+    c.q0 = (g.dimz - g.thd + 4) & ~3;
+    c.nbq = (g.dimz - 4 - c.q0 + 3) / 4;
+    c.nB = g.dimx * (c.ntq + c.nbq);
+    return c;
+}
+constexpr int kStripBlock = 256;          // strip items per block (and per 16-bit ring scale)
+
+__host__ __device__ __forceinline__ int round_block(int n)
+{
+    return (n + kStripBlock - 1) / kStripBlock * kStripBlock;
+}
+
+// Item index of quad (x, zq) in the list above (the quad holding a ring cell).
+__device__ __forceinline__ int strip_item(const Geom &g, const CorrShape &cs, int x, int zq)
+{
+    if (x >= 4 && x < g.thl - 4) return (x - 4) * cs.nql + (zq - 4) / 4;
+    if (x >= g.dimx - g.thr + 4 && x < g.dimx - 4)
+        return (g.thl - 8 + x - (g.dimx - g.thr + 4)) * cs.nql + (zq - 4) / 4;
+    const int k = zq < g.thu - 4 ? (zq - 4) / 4 : cs.ntq + (zq - cs.q0) / 4;
+    return cs.nA + x * (cs.ntq + cs.nbq) + k;
+}
+
+// Cell of ring index r (inverse of ring_index).
+__device__ __forceinline__ void ring_cell(const Geom &g, int r, int &x, int &z)
+{
+    const int w4 = g.ring_w * 4;
+    if (r < w4) { x = g.rx0 - 4 + r / 4; z = g.rz0 - 4 + r % 4; return; }
+    r -= w4;
+    if (r < w4) { x = g.rx0 - 4 + r / 4; z = g.rz1 + r % 4; return; }
+    r -= w4;
+    const int h4 = 4 * g.ring_h;
+    if (r < h4) { x = g.rx0 - 4 + r / g.ring_h; z = g.rz0 + r % g.ring_h; return; }
+    r -= h4;
+    x = g.rx1 + r / g.ring_h;
+    z = g.rz0 + r % g.ring_h;
+}
+
+// One strip quad: the corrections of every strip covering it added to the stencil value
+// that k_mstep stored in u_next, in the reference's order left, top, right, bottom; fv gets
+// the final values.  Returns false for skipped items.
+template <typename T>
+__device__ __forceinline__ bool strip_quad(const BMember<T> &M, const CorrShape &cs, const T *u, T *un,
+                                           int idx, bool fresh, int &x, int &zq, T (&fv)[4])
+{
+    const Geom &g = M.g;
+    const size_t P = (size_t)g.pitch;
+    if (idx < cs.nA) {
+        const int i = idx / cs.nql;
+        x = i < g.thl - 8 ? 4 + i : g.dimx - g.thr + 4 + (i - (g.thl - 8));
+        zq = 4 + 4 * (idx % cs.nql);
+    } else {
+        idx -= cs.nA;
+        const int nq = cs.ntq + cs.nbq;
+        x = idx / nq;
+        const int k = idx % nq;
+        if ((x >= 4 && x < g.thl - 4) || (x >= g.dimx - g.thr + 4 && x < g.dimx - 4)) return false;
+        if (k < cs.ntq) zq = 4 + 4 * k;
+        else {
+            if (x < 4 || x >= g.dimx - 4) return false;
+            zq = cs.q0 + 4 * (k - cs.ntq);
+        }
+    }
+    const bool zx = zq + 4 > 4 && zq < g.dimz - 4;
+    const bool inL = zx && x >= 4 && x < g.thl - 4;
+    const bool inR = zx && x >= g.dimx - g.thr + 4 && x < g.dimx - 4;
+    const bool inT = zq + 4 > 4 && zq < g.thu - 4;                 // every column (the quirk)
+    const bool inB = x >= 4 && x < g.dimx - 4 && zq + 4 > g.dimz - g.thd + 4 && zq < g.dimz - 4;
+    if (!(inL || inR || inT || inB)) return false;
+    T cf[4], cx[4], cz[4];
+    ld4(M.coef + (size_t)x * P + zq, cf);
+    ld4(un + (size_t)x * P + zq, fv);
+    const T *col = u + (size_t)x * P + zq;
+    if (inL || inR) {
+        T W[9][4];
+#pragma unroll
+        for (int m = 0; m < 9; ++m) ld4(col + (ptrdiff_t)(m - 4) * (ptrdiff_t)P, W[m]);
+        if (inL)
+            strip_x_quad<T>(M.psi[0] + (size_t)x * P + zq, M.xi[0] + (size_t)x * P + zq, P, (T)M.prof[0][x],
+                            (T)M.prof[1][x], W, cf, zq, 4, g.dimz - 4, M.h1, M.h2, M.h3, fresh, cx);
+        else {
+            const int li = x - (g.dimx - g.thr);
+            strip_x_quad<T>(M.psi[1] + (size_t)li * P + zq, M.xi[1] + (size_t)li * P + zq, P,
+                            (T)M.prof[2][li], (T)M.prof[3][li], W, cf, zq, 4, g.dimz - 4, M.h1, M.h2,
+                            M.h3, fresh, cx);
+        }
+    }
+    if (inT || inB) {
+        T c4[4], zz[12];
+        ld4(col, c4);
+        {
+            T zm[4], zp[4];
+            ld4(col - 4, zm);
+            ld4(col + 4, zp);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { zz[j] = zm[j]; zz[4 + j] = c4[j]; zz[8 + j] = zp[j]; }
+        }
+        if (inT)
+            strip_z_quad<T>(M.psi[2] + (size_t)x * g.st + zq, M.xi[2] + (size_t)x * g.st + zq, M.prof[4] + zq,
+                            M.prof[5] + zq, zz, cf, zq, 4, g.thu - 4, M.h1, M.h2, M.h3, fresh, cz);
+        else {
+            const int lq = zq - g.zb0;
+            strip_z_quad<T>(M.psi[3] + (size_t)x * g.sb + lq, M.xi[3] + (size_t)x * g.sb + lq, M.prof[6] + lq,
+                            M.prof[7] + lq, zz, cf, zq, g.dimz - g.thd + 4, g.dimz - 4, M.h1, M.h2, M.h3,
+                            fresh, cz);
+        }
+    }
+    // cells outside a strip's z range are left untouched, so that the stored value stays
+    // bit for bit the stencil's
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = zq + j;
+        if (inL && z >= 4 && z < g.dimz - 4) fv[j] = fv[j] + cx[j];
+        if (inT && z >= 4 && z < g.thu - 4) fv[j] = fv[j] + cz[j];
+        if (inR && z >= 4 && z < g.dimz - 4) fv[j] = fv[j] + cx[j];
+        if (inB && z >= g.dimz - g.thd + 4 && z < g.dimz - 4) fv[j] = fv[j] + cz[j];
+    }
+    st4(un + (size_t)x * P + zq, fv);
+    return true;
+}
+
+// After a step's tiles: the CPML corrections of every active field (forward, backward
+// receiver) with the ring storage of the forward field, and the ring restoration of the
+// reconstructed source field.  Member m's items: round_block(strip quads), then
+// round_block(ring cells) -- a block of kStripBlock items never mixes members, so one
+// block's ring cells share one 16-bit scale.  The last CTA advances every member's state.
+template <typename T>
+__global__ void __launch_bounds__(kStripBlock) k_bstrip(const BatchIndex *__restrict__ ix,
+                                                        const BMember<T> *__restrict__ mem,
+                                                        int2 *__restrict__ state, unsigned *__restrict__ done)
+{
+    __shared__ int s_base[kMaxMembers + 1];
+    __shared__ int2 s_state[kMaxMembers];
+    __shared__ float red[kStripBlock / 32];
+    // the next step's k_bpsi may launch; it waits for this grid to complete
+    griddep_launch();
+    const int nmem = ix->nmem;
+    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->corr_base[k];
+    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
+    griddep_wait();                                    // this step's tiles (and psi)
+    __syncthreads();
+    const int n = s_base[nmem];
+    int m = 0;
+    for (int base = blockIdx.x * kStripBlock; base < n; base += gridDim.x * kStripBlock) {
+        while (s_base[m + 1] <= base) ++m;             // block-uniform member
+        const int2 st = s_state[m];
+        const BMember<T> &M = mem[m];
+        const Geom &g = M.g;
+        const bool live = (st.x == 1 || st.x == 2) && st.y < g.nt;
+        const CorrShape cs = corr_shape(g);
+        const int nstrip = round_block(cs.nA + cs.nB);
+        const int local = base - s_base[m];
+        const bool ring = M.storage == 1;
+        if (local < nstrip) {
+            // ---- corrections (+ ring storage of the forward field)
+            const bool save = live && ring && st.x == 1;
+            const int cur = st.y & 1;
+            const T *u = st.x == 1 ? M.u[cur] : M.r[cur];
+            T *un = st.x == 1 ? M.u[1 - cur] : M.r[1 - cur];
+            const int idx = local + threadIdx.x;
+            int x = 0, zq = 0;
+            T fv[4];
+            bool have = false;
+            if (live && idx < cs.nA + cs.nB) have = strip_quad<T>(M, cs, u, un, idx, st.y == 0, x, zq, fv);
+            if (save) {
+                void *slot = member_slot(M, st.y + 1);
+                int ri[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) ri[j] = (have && zq + j < g.dimz) ? ring_index(g, x, zq + j) : -1;
+                if (M.store_prec == 0) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (ri[j] >= 0) reinterpret_cast<T *>(slot)[ri[j]] = fv[j];
+                } else {                               // block-uniform branch
+                    float mx = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (ri[j] >= 0) mx = fmaxf(mx, fabsf((float)fv[j]));
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+                    __syncthreads();
+                    mx = red[0];
+#pragma unroll
+                    for (int w = 1; w < kStripBlock / 32; ++w) mx = fmaxf(mx, red[w]);
+                    __syncthreads();
+                    const float scale = store_scale_of(mx, M.store_prec);
+                    const float inv = 1.0f / scale;
+                    if (threadIdx.x == 0) member_scales(M, st.y + 1)[local / kStripBlock] = scale;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (ri[j] >= 0) store_put<T>(slot, M.store_prec, (size_t)ri[j], fv[j], inv);
+                }
+            }
+        } else if (live && ring && st.x == 2 && st.y >= 2) {
+            // ---- ring cells of the reconstructed source field, from storage slot tau + 1
+            const int r = local - nstrip + threadIdx.x;
+            if (r < g.ring_cells) {
+                const int tau = g.nt - 1 - st.y;
+                const int ua = g.nt & 1, ub = 1 - ua;
+                const int sc = ((st.y - 2) & 1) ? ua : ub, sp = 1 - sc;
+                int x, z;
+                ring_cell(g, r, x, z);
+                float scale = 1.0f;
+                if (M.store_prec != 0)
+                    scale = member_scales(M, tau + 1)[strip_item(g, cs, x, z & ~3) / kStripBlock];
+                M.u[sp][(size_t)x * g.pitch + z] =
+                    store_get<T>(member_slot(M, tau + 1), M.store_prec, (size_t)r, scale);
+            }
+        }
+    }
+    // The last CTA to finish advances every active member by one step: a forward pass has
+    // nt steps, a backward pass nt + 1 (the last one images only).
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned ticket = atomicAdd(done, 1u);
+        if (ticket == gridDim.x - 1) {
+            __threadfence();
+            for (int k = 0; k < nmem; ++k) {
+                int2 st = state[k];
+                if (st.x != 1 && st.x != 2) continue;
+                const int nt = ix->nt[k];
+                ++st.y;
+                if (st.x == 1 && st.y == nt) { st.x = 2; st.y = 0; }
+                else if (st.x == 2 && st.y > nt) { st.x = 3; st.y = 0; }
+                state[k] = st;
+            }
+            atomicExch(done, 0u);
+            __threadfence();
+        }
+    }
 }
 
 // psi update of every active member (one thread per quad of the flattened work list).
@@ -132,6 +469,7 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
         if (st.x != 1 && st.x != 2) continue;
         const BMember<T> &M = mem[m];
         const Geom &g = M.g;
+        if (st.x == 2 && st.y >= g.nt) continue;          // image-only step: no propagation
         int cnt[4];
         psi_counts(g, cnt);
         int lq = q - s_base[m], strip = 0;
@@ -142,101 +480,137 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
     }
 }
 
-template <typename T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2 : 1)
-    k_bstep(const BatchIndex *__restrict__ ix, const BMember<T> *__restrict__ mem,
+// One batched step: every tile of every active member, in two phases (BatchIndex): phase 1
+// = each member's interior field tiles (tile_coords order nb..tiles-1) and, backward with
+// ring storage, its source-field tiles; phase 2 = each member's field tiles touching a CPML
+// strip (tile_coords order 0..nb-1).  Items go to CTAs in chunks of kChunk consecutive items
+// (chunk c to CTA c mod G), so that consecutive items of a CTA mostly share their member and
+// role; an NS-stage TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi
+// of the same step runs alongside, and k_bstrip completes the strip cells afterwards.
+constexpr int kChunk = 4;
+
+template <typename T>
+__global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
+    k_mstep(const BatchIndex *__restrict__ ix, const BMember<T> *__restrict__ mem,
             int2 *__restrict__ state, unsigned *__restrict__ done)
 {
-    using Cfg = StepCfg<T, WARPS, 1>;
-    constexpr int UT = Cfg::UT, PT = Cfg::PT, STAGE = Cfg::STAGE, NS = Cfg::NS, TXC = Cfg::TXC;
+    using Cfg = MCfg<T>;
+    constexpr int UT = Cfg::UT, PT = Cfg::PT, STAGE = Cfg::STAGE, NS = Cfg::NS;
+    static_assert(NS == 2, "two argument slots serve two stages");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *stage0 = reinterpret_cast<T *>(smem_raw);
     __shared__ __align__(8) uint64_t full[NS];
-    __shared__ int tile_of[NS], pass_of[NS];
-    __shared__ StepArgs<T> sargs[NS];
-    __shared__ float red[WARPS];
-    // The work list and the members' (pass, step) of this launch, staged once: the tile ->
-    // member lookups of the issuing thread then stay in shared memory.  state[] is final
-    // here: k_bpsi of this step waited for the previous k_bstep before letting this grid
-    // launch, and the last CTA of this grid rewrites state[] only after every CTA is done.
-    __shared__ int s_base[kMaxMembers + 1];
+    __shared__ int tile_of[NS], role_of[NS], args_of[NS];
+    __shared__ MArgs<T> sargs[2];
+    __shared__ float red[MWARPS];
+    // The work lists and the members' (pass, step) of this launch, staged once.  state[] is
+    // final here: this grid launches after k_bpsi of this step passed its wait on the
+    // previous step, and this grid's last CTA rewrites state[] only after every CTA is done.
+    __shared__ int s_base1[kMaxMembers + 1], s_base2[kMaxMembers + 1];
+    __shared__ short s_tiles[kMaxMembers], s_nb[kMaxMembers];
+    __shared__ int s_nt[kMaxMembers];
     __shared__ int2 s_state[kMaxMembers];
     const int nmem = ix->nmem;
-    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->tile_base[k];
-    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
-
+    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) {
+        s_base1[k] = ix->base1[k];
+        s_base2[k] = ix->base2[k];
+    }
+    for (int k = threadIdx.x; k < nmem; k += blockDim.x) {
+        s_state[k] = state[k];
+        s_tiles[k] = (short)ix->tiles[k];
+        s_nb[k] = (short)ix->nb[k];
+        s_nt[k] = ix->nt[k];
+    }
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
-    const int total = s_base[nmem];
-    // Thread 0 maps the i-th tile of this CTA to (member, local tile), builds the member's
-    // step arguments in shared memory and starts the stage's TMA loads.  The tiles of a CTA
-    // visit the members in increasing order; all tiles of a member share its arguments, so
-    // they are built once per member and copied between stage slots.
-    int cur_m = 0;          // member of the latest tile (monotone)
-    int last_m = -1;        // member whose arguments sit in slot last_slot
-    int last_slot = 0;
-    int l_cur = 0, l_sc = 0, l_sp = 0;
+    const int total1 = s_base1[nmem], total = total1 + s_base2[nmem];
+    // Thread 0 maps the i-th work item of this CTA to (member, role, tile), builds the
+    // arguments of (member, role) when they differ from the last item's (in the argument
+    // slot the other stage is not using) and starts the stage's TMA loads.
+    int cur1 = 0, cur2 = 0;              // member of the latest item of each phase (monotone)
+    int last_key = -1, last_args = 0;
+    int l_mu = 0, l_mp = 0;
     auto issue = [&](int i, int s) {
-        const int tg = blockIdx.x + i * gridDim.x;
+        const int tg = (blockIdx.x + (i / kChunk) * gridDim.x) * kChunk + i % kChunk;
         if (tg >= total) {
+            // past the end: the chunk index only grows, so every later item is too
             tile_of[s] = -1;
             mbar_arrive(&full[s]);
             return;
         }
-        while (s_base[cur_m + 1] <= tg) ++cur_m;
-        const int m = cur_m;
-        const int2 st = s_state[m];
-        if (st.x != 1 && st.x != 2) {     // idle or finished member: nothing to do
+        int m, lt, role;
+        bool skip;
+        if (tg < total1) {
+            while (s_base1[cur1 + 1] <= tg) ++cur1;
+            m = cur1;
+            const int2 st = s_state[m];
+            const int k = tg - s_base1[m], ni = s_tiles[m] - s_nb[m];
+            skip = st.x != 1 && st.x != 2;               // idle or finished member
+            if (k < ni) {
+                role = st.x == 1 ? ROLE_FWD : ROLE_RCV;
+                lt = s_nb[m] + k;
+            } else {
+                role = ROLE_SRC;
+                lt = k - ni;
+                skip = skip || st.x != 2 || st.y < 2 || st.y >= s_nt[m];
+            }
+        } else {
+            const int t2 = tg - total1;
+            while (s_base2[cur2 + 1] <= t2) ++cur2;
+            m = cur2;
+            const int2 st = s_state[m];
+            role = st.x == 1 ? ROLE_FWD : ROLE_RCV;
+            lt = t2 - s_base2[m];
+            skip = st.x != 1 && st.x != 2;
+        }
+        if (skip) {
             tile_of[s] = -2;
             mbar_arrive(&full[s]);
             return;
         }
+        const int2 st = s_state[m];
         const BMember<T> &M = mem[m];
-        if (m != last_m) {
-            // the descriptors were rewritten by the host when the slot was (re)admitted
-            tensormap_acquire(&M.tm_u[0]); tensormap_acquire(&M.tm_u[1]);
-            tensormap_acquire(&M.tm_up[0]); tensormap_acquire(&M.tm_up[1]);
-            tensormap_acquire(&M.tm_r[0]); tensormap_acquire(&M.tm_r[1]);
-            tensormap_acquire(&M.tm_rp[0]); tensormap_acquire(&M.tm_rp[1]);
-            tensormap_acquire(&M.tm_c);
-            member_args<T>(M, st.x, st.y, sargs[s], l_cur, l_sc, l_sp);
-            last_m = m;
-        } else if (last_slot != s) {
-            const int *src = reinterpret_cast<const int *>(&sargs[last_slot]);
-            int *dst = reinterpret_cast<int *>(&sargs[s]);
-#pragma unroll 8
-            for (int k = 0; k < (int)(sizeof(StepArgs<T>) / sizeof(int)); ++k) dst[k] = src[k];
+        const int key = m * 4 + role;
+        if (key != last_key) {
+            if (st.x == 1 && st.y == 0) {
+                // first step after admission: the host has just written this member's tensor
+                // maps; order those writes before their first use by TMA
+                tensormap_acquire(&M.tm_u[0]); tensormap_acquire(&M.tm_u[1]);
+                tensormap_acquire(&M.tm_up[0]); tensormap_acquire(&M.tm_up[1]);
+                tensormap_acquire(&M.tm_r[0]); tensormap_acquire(&M.tm_r[1]);
+                tensormap_acquire(&M.tm_rp[0]); tensormap_acquire(&M.tm_rp[1]);
+                tensormap_acquire(&M.tm_c);
+            }
+            last_args = 1 - args_of[1 - s];          // the slot the other stage is not using
+            margs<T>(M, st.y, role, sargs[last_args], l_mu, l_mp);
+            last_key = key;
         }
-        last_slot = s;
-        const int lt = tg - s_base[m];
+        args_of[s] = last_args;
         tile_of[s] = lt;
-        pass_of[s] = st.x;
-        const Geom &g = sargs[s].g;
+        role_of[s] = role;
         int xt, zt;
-        tile_coords(g, lt, xt, zt);
-        const int x0 = xt * TXC, z0 = ztile_origin(g, zt);
-        const bool recon = st.x == 2 && (sargs[s].flags & F_RECON);
-        const CUtensorMap *mc = st.x == 1 ? &M.tm_u[l_cur] : &M.tm_r[l_cur];
-        const CUtensorMap *mp = st.x == 1 ? &M.tm_up[1 - l_cur] : &M.tm_rp[1 - l_cur];
+        tile_coords(sargs[last_args].g, lt, xt, zt);
+        const int x0 = xt * MTX, z0 = ztile_origin(sargs[last_args].g, zt);
+        const bool rfield = role == ROLE_RCV;
+        const CUtensorMap *mc = rfield ? &M.tm_r[l_mu] : &M.tm_u[l_mu];
+        const CUtensorMap *mp = rfield ? &M.tm_rp[l_mp] : &M.tm_up[l_mp];
         T *stg = stage0 + (size_t)s * STAGE;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(sizeof(T) * (recon ? 2 * UT + 3 * PT : UT + 2 * PT)));
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(sizeof(T) * STAGE));
         tma_load_2d(stg, mc, z0 - HALO, x0 - HALO, &full[s]);
         tma_load_2d(stg + UT, mp, z0, x0, &full[s]);
         tma_load_2d(stg + UT + PT, &M.tm_c, z0, x0, &full[s]);
-        if (recon) {
-            tma_load_2d(stg + UT + 2 * PT, &M.tm_u[l_sc], z0 - HALO, x0 - HALO, &full[s]);
-            tma_load_2d(stg + 2 * UT + 2 * PT, &M.tm_up[l_sp], z0, x0, &full[s]);
-        }
     };
+    if (threadIdx.x == 0) {
+        args_of[0] = args_of[1] = 0;
+    }
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) issue(s, s);
     }
-    griddep_launch();
-    bool psi_ready = false;
+    griddep_launch();                    // k_bstrip of this step may launch; it waits for this grid
     for (int i = 0;; ++i) {
         const int s = i % NS;
         const uint32_t par = (uint32_t)((i / NS) & 1);
@@ -256,32 +630,17 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
         if (lt == -1) break;
         if (lt >= 0) {
             const T *stg = stage0 + (size_t)s * STAGE;
-            if (pass_of[s] == 1) step_tile<T, 0, WARPS>(sargs[s], stg, lt, psi_ready, red);
-            else step_tile<T, 1, WARPS>(sargs[s], stg, lt, psi_ready, red);
+            const int role = role_of[s];
+            const MArgs<T> *ap = &sargs[args_of[s]];
+            if (role == ROLE_FWD) march_tile<T, ROLE_FWD>(ap, stg, lt, red);
+            else if (role == ROLE_RCV) march_tile<T, ROLE_RCV>(ap, stg, lt, red);
+            else march_tile<T, ROLE_SRC>(ap, stg, lt, red);
         }
         __syncthreads();
         if (threadIdx.x == 0) issue(i + NS, s);
     }
-    // The last CTA to finish advances every active member by one step.
+    // Every CTA waits for this step's k_bpsi before it completes, so k_bstrip's wait on this
+    // grid also covers the psi it reads.
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned ticket = atomicAdd(done, 1u);
-        if (ticket == gridDim.x - 1) {
-            griddep_wait();               // k_bpsi of this step has finished reading state[]
-            __threadfence();
-            for (int m = 0; m < ix->nmem; ++m) {
-                int2 st = state[m];
-                if (st.x != 1 && st.x != 2) continue;
-                const int nt = mem[m].g.nt;
-                if (++st.y == nt) {
-                    st.y = 0;
-                    st.x = st.x == 1 ? 2 : 3;
-                }
-                state[m] = st;
-            }
-            atomicExch(done, 0u);
-            __threadfence();
-        }
-    }
+    if (threadIdx.x == 0) griddep_wait();
 }

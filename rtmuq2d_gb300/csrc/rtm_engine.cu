@@ -273,7 +273,8 @@ static Layout make_layout(const rtm_params &p, const Geom &g)
     }
     L.store_bytes = (size_t)L.nslots * L.slot_elems * se;
     L.store = take(L.store_bytes);
-    L.n_scales_per_slot = (size_t)g.tiles_x * g.tiles_z;
+    // 16-bit storage scales of one slot: per tile (snapshots) or per strip block (rings)
+    L.n_scales_per_slot = std::max((size_t)g.tiles_x * g.tiles_z, (size_t)strip_blocks_host(g));
     L.scales = take(p.precision == RTM_PREC_FP32 ? 0 : sizeof(float) * L.nslots * L.n_scales_per_slot);
     const size_t stage = std::max({(size_t)g.dimx * g.dimz, (size_t)std::max(1, p.rec_count) * p.nt,
                                    (size_t)2 * g.nx * g.nz});

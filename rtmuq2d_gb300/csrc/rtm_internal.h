@@ -145,7 +145,9 @@ struct BMember {                 // aligned like its leading tensor maps
     Geom g;
     T h1, h2, h3;
     T *u[2], *r[2];
+    const T *coef;
     T *psi[4], *xi[4];          // left, right, top, bottom
+    T *rec_out;                 // recorded seismogram [irec][nt] (forward; NULL: none)
     const float *prof[8];       // a_l b_l a_r b_r a_t b_t a_b b_b (packed, see ProfLayout)
     const int *rec_last, *rec_first, *rec_cnt;
     const float *wav, *seis_t;
@@ -153,18 +155,28 @@ struct BMember {                 // aligned like its leading tensor maps
     void *store;
     size_t slot_elems;
     float *scales;
+    int scales_per_slot;        // 16-bit storage: scales of one slot (tiles / strip blocks)
     int store_prec, storage;
     unsigned *status;
 };
 
 constexpr int kMaxMembers = 128;   // members of one batch
+constexpr int kBatchTileX = 32;    // x columns per tile of the batched step kernel (MTX)
 
-// Work lists of one batch: member i owns global tiles [tile_base[i], tile_base[i+1]) and
-// psi quads [psi_base[i], psi_base[i+1]).
+// Work lists of one batch.  The tile work of a step runs in two phases: first every
+// member's interior field tiles and source-reconstruction tiles, then every member's field
+// tiles touching a CPML strip.  Member i owns items [base1[i], base1[i+1]) of phase 1 and
+// [base2[i], base2[i+1]) of phase 2, psi quads [psi_base[i], ...) and strip items
+// [corr_base[i], ...) of k_bstrip.
 struct BatchIndex {
     int nmem;
-    int tile_base[kMaxMembers + 1];
-    int psi_base[kMaxMembers + 1];
+    int base1[kMaxMembers + 1];         // phase 1: interior field tiles + source-field tiles
+    int base2[kMaxMembers + 1];         // phase 2: field tiles touching a CPML strip
+    int psi_base[kMaxMembers + 1];      // k_bpsi quads
+    int corr_base[kMaxMembers + 1];     // k_bstrip items
+    int tiles[kMaxMembers];             // field tiles of member i (forward / receiver)
+    int nb[kMaxMembers];                // ...of which touch a strip (tile_coords order first)
+    int nt[kMaxMembers];                // time steps of member i
 };
 
 template <typename T>
@@ -177,17 +189,24 @@ struct PsiArgs {
 };
 
 // ---- batched steps (rtm_batch.cuh) -------------------------------------------------------
-// state[m] = (pass, step): pass 0 idle, 1 forward, 2 backward, 3 finished.
+// state[m] = (pass, step): pass 0 idle, 1 forward (nt steps), 2 backward (nt + 1 steps,
+// the last one images only), 3 finished.
 // done[0]: CTA counter of the step in flight (zero between launches); done[1]: error bits.
 template <typename T>
 cudaError_t launch_bpsi(const BatchIndex *ix, const BMember<T> *mem, const int2 *state, int grid,
                         int pdl, cudaStream_t s);
 template <typename T>
+cudaError_t launch_bstrip(const BatchIndex *ix, const BMember<T> *mem, int2 *state, unsigned *done, int grid,
+                          int pdl, cudaStream_t s);
+template <typename T>
 cudaError_t launch_bstep(const BatchIndex *ix, const BMember<T> *mem, int2 *state, unsigned *done,
                          int grid, int pdl, cudaStream_t s);
 template <typename T>
-int bstep_grid();                                 // persistent CTAs of k_bstep
+int bstep_grid();                                 // persistent CTAs of k_mstep
 void psi_counts_host(const Geom &g, int (&n)[4]);
+int strip_items_host(const Geom &g, int ring);     // k_bstrip items of one member
+int strip_blocks_host(const Geom &g);              // its strip-quad blocks (16-bit ring scales)
+int boundary_tiles_host(const Geom &g);            // field tiles touching a CPML strip
 
 // ---- launchers (rtm_kernels.cu) --------------------------------------------------------
 // pdl: launch with programmatic stream serialization (overlaps the preceding kernel's tail)

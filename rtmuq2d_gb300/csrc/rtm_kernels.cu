@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> 
     psi_quad<T>(a.g, a.h1, a.u, psi, prof, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, false);
 }
 
+#include "rtm_march.cuh"
 #include "rtm_batch.cuh"
 
 // ---- set-up and layout kernels ------------------------------------------------------------
@@ -617,17 +618,50 @@ cudaError_t launch_bpsi(const BatchIndex *ix, const BMember<T> *mem, const int2 
     return cudaLaunchKernelEx(&cfg, k_bpsi<T>, ix, mem, state);
 }
 
-constexpr int kBatchWarps = 8;
+template <typename T>
+cudaError_t launch_bstrip(const BatchIndex *ix, const BMember<T> *mem, int2 *state, unsigned *done, int grid,
+                          int pdl, cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kStripBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute at = pdl_attr();
+    cfg.attrs = pdl ? &at : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    static cudaError_t carve = cudaFuncSetAttribute(k_bstrip<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                    cudaSharedmemCarveoutMaxShared);
+    if (carve != cudaSuccess) return carve;
+    return cudaLaunchKernelEx(&cfg, k_bstrip<T>, ix, mem, state, done);
+}
+
+int strip_items_host(const Geom &g, int ring)
+{
+    const CorrShape c = corr_shape(g);
+    return round_block(c.nA + c.nB) + (ring ? round_block(g.ring_cells) : 0);
+}
+
+int strip_blocks_host(const Geom &g)
+{
+    const CorrShape c = corr_shape(g);
+    return round_block(c.nA + c.nB) / kStripBlock;
+}
+
+int boundary_tiles_host(const Geom &g)
+{
+    const int nzb = g.tiles_z > 1 ? 2 : 1;
+    return g.tiles_x * nzb + (g.nxl + (g.tiles_x - g.xr0)) * (g.tiles_z - nzb);
+}
 
 template <typename T>
 static cudaError_t configure_bstep()
 {
     static cudaError_t state = cudaErrorNotReady;
     if (state == cudaErrorNotReady) {
-        state = cudaFuncSetAttribute(k_bstep<T, kBatchWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)StepCfg<T, kBatchWarps, 1>::SMEM);
+        state = cudaFuncSetAttribute(k_mstep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)MCfg<T>::SMEM);
         if (state == cudaSuccess)
-            state = cudaFuncSetAttribute(k_bstep<T, kBatchWarps>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            state = cudaFuncSetAttribute(k_mstep<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                          cudaSharedmemCarveoutMaxShared);
     }
     return state;
@@ -642,8 +676,7 @@ int bstep_grid()
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bstep<T, kBatchWarps>, kBatchWarps * 32,
-                                                      StepCfg<T, kBatchWarps, 1>::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mstep<T>, MTHREADS, MCfg<T>::SMEM);
         grid = (per_sm < 1 ? 1 : per_sm) * sms;
     }
     return grid;
@@ -657,19 +690,21 @@ cudaError_t launch_bstep(const BatchIndex *ix, const BMember<T> *mem, int2 *stat
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kBatchWarps * 32);
-    cfg.dynamicSmemBytes = StepCfg<T, kBatchWarps, 1>::SMEM;
+    cfg.blockDim = dim3(MTHREADS);
+    cfg.dynamicSmemBytes = MCfg<T>::SMEM;
     cfg.stream = s;
     cudaLaunchAttribute at = pdl_attr();
     cfg.attrs = pdl ? &at : nullptr;
     cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_bstep<T, kBatchWarps>, ix, mem, state, done);
+    return cudaLaunchKernelEx(&cfg, k_mstep<T>, ix, mem, state, done);
 }
 
 template cudaError_t launch_bpsi<float>(const BatchIndex *, const BMember<float> *, const int2 *, int, int,
                                         cudaStream_t);
 template cudaError_t launch_bstep<float>(const BatchIndex *, const BMember<float> *, int2 *, unsigned *,
                                          int, int, cudaStream_t);
+template cudaError_t launch_bstrip<float>(const BatchIndex *, const BMember<float> *, int2 *, unsigned *, int,
+                                          int, cudaStream_t);
 template int bstep_grid<float>();
 
 #define RTM_INSTANTIATE(T)                                                                      \

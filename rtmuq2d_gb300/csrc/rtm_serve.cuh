@@ -5,9 +5,9 @@
 // in arrival order while a member slot is free and their device footprint fits the HBM
 // budget; admission uploads the inputs and sets the member up (coef, seismogram transpose,
 // zeroed wavefields and image accumulators).  rtm_server_step replays a CUDA graph of
-// `steps_per_launch` batched time steps (k_bpsi + k_bstep per step, chained by programmatic
-// dependent launch): every active member advances one step per batched step, whatever its
-// grid, time axis or pass.  Members that finished their backward pass are harvested (image
+// `steps_per_launch` batched time steps (k_bpsi + k_mstep + k_bstrip per step, chained by
+// programmatic dependent launch): every active member advances one step per batched step,
+// whatever its grid, time axis or pass.  Members that finished their backward pass are harvested (image
 // and self image copied to host buffers) and their slots freed for the next admissions --
 // continuous batching.  One thread drives a server; each server has its own stream.
 
@@ -75,6 +75,7 @@ static void member_from_plan(rtm_plan *P, BMember<float> &M)
     M.h3 = 1.0f / (dx * dx);
     M.u[0] = P->at<float>(P->L.u[0]); M.u[1] = P->at<float>(P->L.u[1]);
     M.r[0] = P->at<float>(P->L.r[0]); M.r[1] = P->at<float>(P->L.r[1]);
+    M.coef = P->at<float>(P->L.coef);
     for (int k = 0; k < 4; ++k) {
         M.psi[k] = P->at<float>(P->L.psi[k]);
         M.xi[k] = P->at<float>(P->L.xi[k]);
@@ -91,6 +92,7 @@ static void member_from_plan(rtm_plan *P, BMember<float> &M)
     M.store = P->base + P->L.store;
     M.slot_elems = P->L.slot_elems;
     M.scales = P->p.precision == RTM_PREC_FP32 ? nullptr : P->at<float>(P->L.scales);
+    M.scales_per_slot = (int)P->L.n_scales_per_slot;
     M.store_prec = P->p.precision;
     M.storage = P->p.storage;
     M.status = P->at<unsigned>(P->L.status);
@@ -102,24 +104,38 @@ static int server_fail(rtm_server *S, int code)
     return code;
 }
 
-// Work lists of the current membership (inactive slots own no tiles).
+// Work lists of the current membership (inactive slots own no work).
 static void rebuild_index(rtm_server *S)
 {
     S->ix.nmem = S->max_members;
-    int tb = 0, pb = 0;
+    int b1 = 0, b2 = 0, pb = 0, cb = 0;
     for (int m = 0; m < S->max_members; ++m) {
-        S->ix.tile_base[m] = tb;
+        S->ix.base1[m] = b1;
+        S->ix.base2[m] = b2;
         S->ix.psi_base[m] = pb;
+        S->ix.corr_base[m] = cb;
+        S->ix.tiles[m] = 0;
+        S->ix.nb[m] = 0;
+        S->ix.nt[m] = 0;
         if (S->slot_plan[m]) {
-            const Geom &g = S->slot_plan[m]->g;
+            const rtm_plan *P = S->slot_plan[m];
+            const Geom &g = P->g;
             int n[4];
             psi_counts_host(g, n);
-            tb += g.tiles;
+            const int nb = boundary_tiles_host(g);
+            b1 += (g.tiles - nb) + (P->p.storage == RTM_STORE_RING ? g.tiles : 0);
+            b2 += nb;
             pb += n[0] + n[1] + n[2] + n[3];
+            cb += strip_items_host(g, P->p.storage == RTM_STORE_RING);
+            S->ix.tiles[m] = g.tiles;
+            S->ix.nb[m] = nb;
+            S->ix.nt[m] = g.nt;
         }
     }
-    S->ix.tile_base[S->max_members] = tb;
+    S->ix.base1[S->max_members] = b1;
+    S->ix.base2[S->max_members] = b2;
     S->ix.psi_base[S->max_members] = pb;
+    S->ix.corr_base[S->max_members] = cb;
 }
 
 // Sets up one admitted request in slot m on the server's stream.
@@ -147,6 +163,8 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
         P->own_stream = false;
     }
     const Geom &g = P->g;
+    if (g.tx != kBatchTileX)              // tensor-map boxes must match the kernel's tiles
+        return fail(RTM_ERR_INVALID, "batched member with tile width %d (needs %d)", g.tx, kBatchTileX);
     cudaStream_t s = S->stream;
     float *stage = P->at<float>(P->L.staging);
     float *h;
@@ -230,6 +248,8 @@ static int capture_graph(rtm_server *S)
     for (int k = 0; k < S->steps_per_launch && e == cudaSuccess; ++k) {
         e = launch_bpsi<float>(S->d_ix, S->d_mem, S->d_state, pgrid, k > 0, S->stream);
         if (e == cudaSuccess) e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, 1, S->stream);
+        if (e == cudaSuccess)
+            e = launch_bstrip<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, pgrid, 1, S->stream);
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(S->stream, &graph);
@@ -314,11 +334,14 @@ int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity,
     if (!S || !p || !velocity) return fail(RTM_ERR_INVALID, "null argument");
     RTM_TRY(check_params(*p));
     if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "the server runs FP32 migrations");
-    const long long bytes = rtm_footprint_bytes(p);
+    rtm_params q = *p;
+    q.tile_x = kBatchTileX;
+    const long long bytes = rtm_footprint_bytes(&q);
     if (bytes > S->budget) return fail(RTM_ERR_NOMEM, "request needs %lld bytes, budget %lld", bytes, S->budget);
     auto *R = new ServeRequest();
     R->id = S->next_id++;
     R->p = *p;
+    R->p.tile_x = kBatchTileX;           // the batched step kernel's tile width
     const size_t nv = (size_t)(p->th_left + p->nx + p->th_right) * (p->th_up + p->nz + p->th_down);
     R->vel.assign(velocity, velocity + nv);
     if (p->n_wavelet > 0) R->wav.assign(wavelet, wavelet + p->n_wavelet);
@@ -362,7 +385,7 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
         RTM_CUDA(cudaEventRecord(S->ev0, S->stream));
         RTM_CUDA(cudaGraphLaunch(S->gexec, S->stream));
         RTM_CUDA(cudaEventRecord(S->ev1, S->stream));
-        S->launches += 2LL * S->steps_per_launch;
+        S->launches += 3LL * S->steps_per_launch;
         RTM_CUDA(cudaMemcpyAsync(S->h_state, S->d_state, sizeof(int2) * S->max_members,
                                  cudaMemcpyDeviceToHost, S->stream));
         RTM_CUDA(cudaStreamSynchronize(S->stream));

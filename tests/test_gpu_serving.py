@@ -1,6 +1,7 @@
 """Serving / batching engine (rtm_server_*): resident migrations advanced together by the
-batched step kernels must give the same images as one migration run alone through
-rtm_migrate_shot (same tiles, same arithmetic: bit-identical), whatever the mix they run in.
+batched step kernels.  Each image matches the reference's (rel-L2 <= 1e-4) and the
+single-migration path (<= 1e-5: same scheme, other tiling), and a migration's image is the
+same bit for bit whether it runs alone or in a mix of other grids, time axes and storages.
 """
 import numpy as np
 import pytest
@@ -41,22 +42,27 @@ def test_server_single_request_equals_migrate_shot(engine, name, storage):
     except engine.RtmError:
         pytest.skip("shot outside the reconstruction region for this case")
     ref_img, ref_slf = engine.migrate_shot(p, ext, wav, seis)
-    srv = engine.Server(0, max_members=4, steps_per_launch=16)
-    rid = srv.submit(p, ext, wav, seis)
-    out = srv.run_all()
-    img, slf, times = out[rid]
-    srv.close()
-    assert np.array_equal(img, ref_img)
-    assert np.array_equal(slf, ref_slf)
+    img, slf, times = _alone(engine, (p, ext, wav, seis))
     assert rel_l2(img, d[name + "/image"]) <= 1e-4
+    assert rel_l2(slf, d[name + "/self"]) <= 1e-4
+    assert rel_l2(img, ref_img) <= 1e-5
+    assert rel_l2(slf, ref_slf) <= 1e-5
     assert times[0] <= times[1] <= times[2]
+
+
+def _alone(engine, case):
+    srv = engine.Server(0, max_members=4, steps_per_launch=16)
+    rid = srv.submit(*case)
+    out = srv.run_all()
+    srv.close()
+    return out[rid]
 
 
 def test_server_mixed_batch_equals_each_alone(engine):
     d = load()
     cases = _mix(engine, d)
     assert all(_valid(engine, c[0]) for c in cases)
-    solo = [engine.migrate_shot(*c) for c in cases]
+    solo = [_alone(engine, c)[:2] for c in cases]
     # fewer slots than requests: members finish and new ones are admitted mid-run;
     # steps_per_launch not dividing any nt: members finish inside a graph replay
     srv = engine.Server(0, max_members=3, steps_per_launch=7)
@@ -88,7 +94,7 @@ def test_server_admission_respects_budget(engine):
             r = srv.poll()
     assert max(seen) == 1                     # one footprint fits the budget at a time
     assert srv.stats()["bytes_in_use"] <= int(fp * 1.5)
-    ref, _ = engine.migrate_shot(*cases[0])
+    ref = _alone(engine, cases[0])[0]
     for rid in ids:
         assert np.array_equal(out[rid][0], ref)
     big = cases[0][0].replace(nx=cases[0][0].nx * 4)
