@@ -340,7 +340,7 @@ __device__ __forceinline__ bool strip_quad(const BMember<T> &M, const CorrShape 
 // round_block(ring cells) -- a block of kStripBlock items never mixes members, so one
 // block's ring cells share one 16-bit scale.  The last CTA advances every member's state.
 template <typename T>
-__global__ void __launch_bounds__(kStripBlock) k_bstrip(const BatchIndex *__restrict__ ix,
+__global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__restrict__ ix,
                                                         const BMember<T> *__restrict__ mem,
                                                         int2 *__restrict__ state, unsigned *__restrict__ done)
 {
