@@ -61,6 +61,8 @@ def parse():
                     help="arrival rate as a fraction of the batched service capacity")
     ap.add_argument("--steps-per-launch", type=int, default=16,
                     help="batched steps per CUDA-graph replay of the server")
+    ap.add_argument("--precision-nt", type=int, default=7500,
+                    help="reduced-precision storage study: time steps (0: skip)")
     return ap.parse_args()
 
 
@@ -335,6 +337,69 @@ def run_served(args, eng, capacity_gcells):
             "ring_precisions": ["fp32", "bf16"], "gpu_launches": st["launches"]}
 
 
+def run_precision(args, eng):
+    """Reduced-precision source storage on the 3400 x 700 grid and shot, imaging every 4th
+    step: FP32 / BF16 / FP16 boundary rings and imaging-interval snapshots (per-step max-abs
+    scales for 16-bit), stencil and CPML in FP32, image accumulated in FP64; relative L2
+    error of the image, and of the reconstructed source wavefield at t = 0.5, 1.5, 2.5 s,
+    against an FP64 run of the identical scheme."""
+    import torch
+    from rtmuq2d_gb300 import workloads
+    p0 = workloads.params_large(time_slices=4, nt=args.precision_nt)
+    true, mig = workloads.models_large(p0, seed=1)
+    wav = workloads.wavelet_for(p0)
+    ext_true = eng.extend_matrix(p0, true)
+    ext = eng.extend_matrix(p0, mig)
+    seis = eng.model_seismogram(p0.replace(storage=0), ext_true, wav)
+    times = [t for t in (int(round(s / p0.dt)) for s in (0.5, 1.5, 2.5)) if t <= p0.nt - 2]
+    d_vel = torch.from_numpy(ext).cuda()
+    d_wav = torch.from_numpy(wav).cuda()
+    d_seis = torch.from_numpy(seis).cuda()
+
+    def run(p):
+        fdt = torch.float64 if p.compute else torch.float32
+        plan = eng.Plan(p)
+        cap = None
+        if p.storage == eng.STORE_RING and times:
+            cap = torch.zeros((len(times), p.dim_x, p.dim_z), dtype=fdt, device="cuda")
+            plan.capture_source(times, cap)
+        t0 = time.perf_counter()
+        plan.forward(d_vel, d_wav)
+        plan.adjoint(d_seis)
+        plan.sync()
+        secs = time.perf_counter() - t0
+        img = torch.zeros((p.nx, p.nz), dtype=torch.float64, device="cuda")
+        plan.read_image(0, img, as_double=True)
+        plan.sync()
+        out = (img.cpu().numpy(), cap.cpu().numpy().astype(np.float64) if cap is not None else None, secs)
+        del plan
+        eng.release_cached()
+        return out
+
+    inner = (slice(p0.th_left, p0.th_left + p0.nx), slice(p0.th_up, p0.th_up + p0.nz))
+
+    def rel(a, b):
+        den = float(np.linalg.norm(b))
+        return float(np.linalg.norm(a - b) / den) if den > 0 else None
+
+    ref_img, ref_fields, ref_s = run(p0.replace(storage=eng.STORE_RING, compute=eng.COMPUTE_FP64))
+    names = {eng.PREC_FP32: "fp32", eng.PREC_BF16: "bf16", eng.PREC_FP16: "fp16"}
+    variants = []
+    for storage, sname in ((eng.STORE_RING, "ring"), (eng.STORE_SNAPSHOT, "snapshot")):
+        for prec in (eng.PREC_FP32, eng.PREC_BF16, eng.PREC_FP16):
+            img, fields, secs = run(p0.replace(storage=storage, precision=prec))
+            v = {"storage": sname, "precision": names[prec], "image_rel_l2_vs_fp64": rel(img, ref_img),
+                 "seconds": secs,
+                 "store_bytes": int(eng.footprint_bytes(p0.replace(storage=storage, precision=prec)))}
+            if fields is not None:
+                # the reconstruction rebuilds the model interior (not the CPML): compare there
+                v["field_rel_l2_vs_fp64"] = {"t=%.1fs" % (t * p0.dt): rel(fields[k][inner], ref_fields[k][inner])
+                                             for k, t in enumerate(times)}
+            variants.append(v)
+    return {"workload": "precision_3400x700_nt%d_imaging_every_4" % p0.nt, "reference": "fp64 run, ring storage",
+            "fp64_seconds": ref_s, "variants": variants}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -500,6 +565,9 @@ def run_gpu(args):
         served["clocks"] = smp.summary()
         served["plain_value"] = value
         served["speedup_vs_plain"] = served["value"] / value
+    precision = None
+    if ws == 1 and args.precision_nt > 0:
+        precision = run_precision(args, eng)
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
@@ -517,7 +585,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
                     "entry_point": "rtm_migrate_shot", "image_agreement_rel_l2": agree},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": sampler.summary(), "batched": batched, "served": served}
+            "clocks": sampler.summary(), "batched": batched, "served": served, "precision": precision}
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

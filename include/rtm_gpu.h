@@ -174,6 +174,13 @@ int rtm_plan_read_field(rtm_plan *plan, int which, void *d_out);
 /* image (which = 0) or self image (which = 1), nx x nz, float or double, to a device
  * buffer; valid after rtm_plan_adjoint. */
 int rtm_plan_read_image(rtm_plan *plan, int which, int as_double, void *d_out);
+/* Captures the source wavefield as the next rtm_plan_adjoint holds it at forward times
+ * times[0..count) (0 <= t <= nt): u_nt and u_{nt-1} are the forward pass's last fields, u_t for
+ * t <= nt-2 the boundary-ring reconstruction (RTM_STORE_RING only).  d_out: count dimX x dimZ
+ * fields (x-major, compute type), written during the adjoint pass.  count = 0 clears.  No
+ * counterpart in the reference; used to measure the reconstruction's error per storage
+ * precision.  Time loops run without CUDA graphs while captures are set. */
+int rtm_plan_capture_source(rtm_plan *plan, int count, const int *times, void *d_out);
 /* Waits for the plan's stream and reports a device-side failure flag. */
 int rtm_plan_sync(rtm_plan *plan);
 /* Number of kernels the plan launched since creation (launch accounting). */

@@ -154,6 +154,7 @@ def _declare(L):
         "rtm_plan_read_field": (C.c_int, [vp, C.c_int, vp]),
         "rtm_plan_read_image": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "rtm_plan_sync": (C.c_int, [vp]),
+        "rtm_plan_capture_source": (C.c_int, [vp, C.c_int, ip, vp]),
         "rtm_plan_launch_count": (C.c_longlong, [vp]),
         "rtm_plan_bytes": (C.c_longlong, [vp]),
         "rtm_release_cached": (None, []),
@@ -188,7 +189,8 @@ def exported_symbols():
             "rtm_aiso_attenuation_cpml", "rtm_attenuation_profile_cpml", "rtm_extend_matrix",
             "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_plan_create",
             "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
-            "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_launch_count",
+            "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_capture_source",
+            "rtm_plan_launch_count",
             "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
             "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_step",
             "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static",
@@ -390,6 +392,12 @@ class Plan:
 
     def sync(self):
         _check(lib().rtm_plan_sync(self.handle))
+
+    def capture_source(self, times, d_out=None):
+        """Source wavefield of the next adjoint pass at forward times `times` into d_out
+        (len(times) x dimX x dimZ device elements of the compute type); [] clears."""
+        t = (C.c_int * max(1, len(times)))(*times)
+        _check(lib().rtm_plan_capture_source(self.handle, len(times), t, _dev(d_out)))
 
     def profile(self, every: int):
         _check(lib().rtm_plan_profile(self.handle, every))

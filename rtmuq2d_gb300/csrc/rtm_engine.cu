@@ -318,6 +318,9 @@ struct rtm_plan {
     long long graph_launches[2] = {0, 0};
     int capture_pass = -1;       // pass being captured (0 forward, 1 backward), or -1
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> graph_events[2];
+    // source-field captures of the next adjoint pass (rtm_plan_capture_source)
+    std::vector<int> cap_times;
+    void *cap_out = nullptr;
 
     template <typename T> T *at(size_t off) { return reinterpret_cast<T *>(base + off); }
 
@@ -664,6 +667,21 @@ static int run_adjoint(rtm_plan *P, const float *d_seis)
     const bool ring = P->p.storage == RTM_STORE_RING;
     const int ua = P->cur_u, ub = 1 - P->cur_u;   // u_nt, u_{nt-1}
     (void)step_grid<T>(1, g);            // configure the kernels before any capture
+    // source-field captures: u_nt and u_{nt-1} are the forward pass's last fields; u_t for
+    // t <= nt - 2 is the reconstruction output of backward step nt - t
+    const size_t cap_n = (size_t)g.dimx * g.dimz;
+    auto capture = [&](int t, const T *field) -> int {
+        for (size_t k = 0; k < P->cap_times.size(); ++k)
+            if (P->cap_times[k] == t) {
+                RTM_CUDA(launch_field_out<T>(g, field, static_cast<T *>(P->cap_out) + k * cap_n, s));
+                P->launches++;
+            }
+        return RTM_OK;
+    };
+    if (!P->cap_times.empty()) {
+        RTM_TRY(capture(g.nt, u[ua]));
+        RTM_TRY(capture(g.nt - 1, u[ub]));
+    }
     auto loop = [&]() -> int {
         int sc = ub, sp = ua;                          // reconstruction: current / previous
         int c = 0;
@@ -715,11 +733,12 @@ static int run_adjoint(rtm_plan *P, const float *d_seis)
             RTM_TRY(timed_step<T>(P, 1, time, maps, a));
             P->launches += 2;
             c ^= 1;
+            if (recon && !P->cap_times.empty()) RTM_TRY(capture(g.nt - time, u[sp]));
             if (recon) std::swap(sc, sp);
         }
         return RTM_OK;
     };
-    RTM_TRY(run_loop(P, 1, true, loop));
+    RTM_TRY(run_loop(P, 1, P->cap_times.empty(), loop));
     const int c = g.nt & 1;             // r buffer holding the last receiver field
     P->cur_r = c;
     P->forward_done = false;   // the stored source wavefield has been consumed
@@ -956,6 +975,19 @@ int rtm_plan_read_field(rtm_plan *plan, int which, void *d_out)
     else RTM_CUDA(launch_field_out<float>(plan->g, plan->at<float>(off), (float *)d_out, plan->stream));
     plan->launches++;
     RTM_CUDA(cudaStreamSynchronize(plan->stream));
+    return RTM_OK;
+}
+
+int rtm_plan_capture_source(rtm_plan *P, int count, const int *times, void *d_out)
+{
+    if (!P) return fail(RTM_ERR_INVALID, "null plan");
+    if (count < 0 || (count > 0 && (!times || !d_out))) return fail(RTM_ERR_INVALID, "bad capture list");
+    if (count > 0 && P->p.storage != RTM_STORE_RING)
+        return fail(RTM_ERR_INVALID, "source-field capture needs ring storage (the reconstructed field)");
+    for (int k = 0; k < count; ++k)
+        if (times[k] < 0 || times[k] > P->p.nt) return fail(RTM_ERR_INVALID, "capture time %d outside [0, nt]", times[k]);
+    P->cap_times.assign(times, times + count);
+    P->cap_out = count > 0 ? d_out : nullptr;
     return RTM_OK;
 }
 

@@ -182,3 +182,37 @@ def test_16bit_storage_close_to_fp32(engine, storage, precision, tol):
     err = rel_l2(img, ref)
     assert err <= tol, err
     assert err > 0.0          # the 16-bit path really ran
+
+
+@pytest.mark.parametrize("compute,tol", ((1, 1e-9), (0, 2e-3)))
+def test_reconstructed_source_field_matches_forward(engine, oracle, compute, tol):
+    """The boundary-ring reconstruction rebuilds the forward wavefield in reverse time inside
+    the reconstruction region (outside it, in the CPML, the field is not rebuilt): the source
+    field captured during the adjoint pass at forward times 21 and 101 equals the forward
+    field u_t (the oracle's snapshot of step t-1, same precision) over the model interior."""
+    import torch
+    d = load()
+    p = _params(engine, d, "uneven", storage=1, compute=compute)
+    dt = torch.float64 if compute else torch.float32
+    npd = np.float64 if compute else np.float32
+    ext, wav, seis = d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"]
+    fwd = oracle.forward(p.as_dict(), ext, wav, snapshots=True, dtype=npd)
+    times = [21, 101, p.nt - 1, p.nt]
+    plan = engine.Plan(p)
+    out = torch.zeros((len(times), p.dim_x, p.dim_z), dtype=dt, device="cuda")
+    plan.capture_source(times, out)
+    dv = torch.from_numpy(ext).cuda()
+    plan.forward(dv, torch.from_numpy(wav).cuda())
+    img = torch.zeros((p.nx, p.nz), dtype=dt, device="cuda")
+    slf = torch.zeros_like(img)
+    plan.adjoint(torch.from_numpy(seis).cuda(), img, slf)
+    plan.sync()
+    got = out.cpu().numpy()
+    inner = (slice(p.th_left, p.th_left + p.nx), slice(p.th_up, p.th_up + p.nz))
+    for k, t in enumerate(times[:2]):
+        ref = fwd["snapshots"][(t - 1) // p.time_slices]
+        err = rel_l2(got[k][inner], ref[inner])
+        assert err <= tol, (t, err)
+    # u_{nt-1} and u_nt: the forward pass's last two fields, before any reconstruction
+    assert rel_l2(got[2], fwd["u_prev"]) <= (1e-12 if compute else 1e-5)
+    assert rel_l2(got[3], fwd["u_last"]) <= (1e-12 if compute else 1e-5)
