@@ -443,6 +443,11 @@ def run_gpu(args):
     p, ext_true, ext, wav = workload(args)
     # observed data: forward modelling on the true model with trace recording (untimed)
     seis = eng.model_seismogram(p.replace(storage=0), ext_true, wav)
+    # step-kernel tile width for this grid shape (plans below use it: tile_x = 0)
+    tuned = None
+    if not args.tile_x:
+        tx, ms = eng.autotune(p, 200)
+        tuned = {"tile_x": tx, "ms_per_forward_step": ms}
 
     stream = torch.cuda.Stream()
     plan = eng.Plan(p)
@@ -578,7 +583,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
                        "receivers": p.rec_count, "storage": args.storage, "ring_precision": "fp32",
-                       "parallelism": "replicas" if ws > 1 else "single",
+                       "parallelism": "replicas" if ws > 1 else "single", "autotuned": tuned,
                        "l2": "flushed between timed iterations (256 MB write)"},
             "e2e": {"value": e2e_value, "unit": "Gcell-updates/s", "ms_per_step": e2e_total / args.steps,
                     "h2d_bytes_per_step": int(ext.nbytes + wav.nbytes + seis.nbytes),

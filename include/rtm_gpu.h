@@ -155,6 +155,14 @@ int rtm_laplacian_filter2D(const rtm_params *p, float *lp, const float *image);
 int rtm_normalized_cross_correlation(const rtm_params *p, float *image, float *self_image,
                                      const float *source, const float *receiver);
 
+/* ---- tile-width autotuning ---------------------------------------------------------------
+ * Times `steps` forward steps of *p's grid shape for every tile width the step kernel
+ * supports (8, 16, 32 columns: 4, 8, 16 warps per CTA; FP64 up to 16) and remembers the
+ * fastest for that shape (grid, CPML, storage, precision, compute): every plan created
+ * afterwards with tile_x = 0 for that shape uses it.  Returns the choice and its time per
+ * step.  Process-wide, thread-safe.  No counterpart in the reference. */
+int rtm_autotune(const rtm_params *p, int steps, int *best_tile_x, float *ms_per_step);
+
 /* ---- device-resident plan (inputs already in HBM) ------------------------------------ */
 typedef struct rtm_plan rtm_plan;
 

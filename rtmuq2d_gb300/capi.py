@@ -146,6 +146,7 @@ def _declare(L):
         "rtm_extend_matrix": (None, [P, fp, fp]),
         "rtm_laplacian_filter2D": (C.c_int, [P, fp, fp]),
         "rtm_normalized_cross_correlation": (C.c_int, [P, fp, fp, fp, fp]),
+        "rtm_autotune": (C.c_int, [P, C.c_int, ip, C.POINTER(C.c_float)]),
         "rtm_plan_create": (C.c_int, [P, C.POINTER(vp)]),
         "rtm_plan_destroy": (C.c_int, [vp]),
         "rtm_plan_set_stream": (C.c_int, [vp, vp]),
@@ -187,7 +188,7 @@ def exported_symbols():
             "rtm_last_error", "rtm_device_info", "rtm_forward_modeling", "rtm_adjoint_modeling",
             "rtm_migrate_shot", "rtm_model_seismogram", "rtm_iso_acoustic_wave_equation",
             "rtm_aiso_attenuation_cpml", "rtm_attenuation_profile_cpml", "rtm_extend_matrix",
-            "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_plan_create",
+            "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_autotune", "rtm_plan_create",
             "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
             "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_capture_source",
             "rtm_plan_launch_count",
@@ -347,6 +348,15 @@ def dropin_lib():
     """librtm_dropin.so: the reference's entry-point names over the engine."""
     lib()
     return C.CDLL(_build.DROPIN_LIB)
+
+
+def autotune(p: RtmParams, steps: int = 200):
+    """Fastest step-kernel tile width for p's grid shape (used by later plans with tile_x = 0);
+    returns (tile_x, ms per forward step)."""
+    t = C.c_int()
+    ms = C.c_float()
+    _check(lib().rtm_autotune(C.byref(p), steps, C.byref(t), C.byref(ms)))
+    return t.value, ms.value
 
 
 def release_cached() -> None:

@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "rtm_gpu.h"
@@ -94,10 +95,31 @@ static int make_field_map(CUtensorMap *m, void *base, const Geom &g, size_t es)
 // ---- geometry and validation ----------------------------------------------------------------
 static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
+// ---- tile-width autotuning (rtm_autotune) ---------------------------------------------------
+// Best tile width per grid shape, measured by rtm_autotune and used by every plan of that
+// shape created afterwards with tile_x = 0.
+struct TuneKey {
+    int dimx, dimz, thl, thr, thu, thd, storage, precision, compute;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(dimx, dimz, thl, thr, thu, thd, storage, precision, compute) <
+               std::tie(o.dimx, o.dimz, o.thl, o.thr, o.thu, o.thd, o.storage, o.precision, o.compute);
+    }
+};
+static std::mutex g_tune_mutex;
+static std::map<TuneKey, int> g_tuned;
+
+static TuneKey tune_key(const rtm_params &p)
+{
+    return {p.th_left + p.nx + p.th_right, p.th_up + p.nz + p.th_down, p.th_left, p.th_right, p.th_up,
+            p.th_down, p.storage, p.precision, p.compute};
+}
+
 static int default_tile_x(const rtm_params &p)
 {
-    (void)p;
-    return 16;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(tune_key(p));
+    return it != g_tuned.end() ? it->second : 16;
 }
 
 static Geom make_geom(const rtm_params &p)
@@ -914,6 +936,62 @@ int rtm_device_info(char *name, int name_len, int *sm_count, long long *hbm_byte
     if (name && name_len > 0) snprintf(name, name_len, "%s", prop.name);
     if (sm_count) *sm_count = prop.multiProcessorCount;
     if (hbm_bytes) *hbm_bytes = (long long)prop.totalGlobalMem;
+    return RTM_OK;
+}
+
+// Times `steps` forward steps of *p's grid (constant 2000 m/s medium, the configured source)
+// for each tile width the step kernel supports and keeps the fastest for this grid shape.
+int rtm_autotune(const rtm_params *p, int steps, int *best_tile_x, float *best_ms_per_step)
+{
+    if (!p) return fail(RTM_ERR_INVALID, "null argument");
+    RTM_TRY(check_params(*p));
+    if (steps < 1) return fail(RTM_ERR_INVALID, "steps must be >= 1");
+    rtm_params q = *p;
+    q.nt = (steps + q.time_slices - 1) / q.time_slices * q.time_slices;
+    const int cands[3] = {8, 16, 32};
+    int best = -1;
+    float best_ms = 0.0f;
+    for (int tx : cands) {
+        if (q.compute == RTM_COMPUTE_FP64 && tx > 16) continue;
+        q.tile_x = tx;
+        rtm_plan *P = nullptr;
+        int st = plan_alloc(q, &P);
+        if (st != RTM_OK) return st;
+        const size_t nv = (size_t)P->g.dimx * P->g.dimz;
+        float *d_vel = nullptr, *d_wav = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float ms = 0.0f;
+        std::vector<float> hv(nv, 2000.0f), hw((size_t)std::max(q.n_wavelet, 1), 0.0f);
+        for (size_t k = 0; k < hw.size(); ++k) hw[k] = (k % 7) * 0.1f;
+        cudaError_t e = cudaMalloc(&d_vel, nv * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&d_wav, hw.size() * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpy(d_vel, hv.data(), nv * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_wav, hw.data(), hw.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        for (int rep = 0; rep < 2 && e == cudaSuccess && st == RTM_OK; ++rep) {
+            e = cudaEventRecord(e0, P->stream);
+            if (e == cudaSuccess) st = dispatch_forward(P, d_vel, P->g.dimz, d_wav, nullptr);
+            if (e == cudaSuccess && st == RTM_OK) e = cudaEventRecord(e1, P->stream);
+            if (e == cudaSuccess && st == RTM_OK) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess && st == RTM_OK) e = cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(d_vel);
+        cudaFree(d_wav);
+        plan_free(P);
+        if (st != RTM_OK) return st;
+        if (e != cudaSuccess) return fail(RTM_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+        const float per = ms / (float)q.nt;
+        if (best < 0 || per < best_ms) { best = tx; best_ms = per; }
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tuned[tune_key(*p)] = best;
+    }
+    if (best_tile_x) *best_tile_x = best;
+    if (best_ms_per_step) *best_ms_per_step = best_ms;
     return RTM_OK;
 }
 

@@ -216,3 +216,12 @@ def test_reconstructed_source_field_matches_forward(engine, oracle, compute, tol
     # u_{nt-1} and u_nt: the forward pass's last two fields, before any reconstruction
     assert rel_l2(got[2], fwd["u_prev"]) <= (1e-12 if compute else 1e-5)
     assert rel_l2(got[3], fwd["u_last"]) <= (1e-12 if compute else 1e-5)
+
+
+def test_autotune_picks_a_width_and_plans_stay_correct(engine):
+    d = load()
+    p = _params(engine, d, "uneven", storage=1)
+    tx, ms = engine.autotune(p, steps=40)
+    assert tx in (8, 16, 32) and ms > 0
+    img, _ = engine.migrate_shot(p, d["uneven/ext"], d["uneven/wavelet"], d["uneven/seis"])
+    assert rel_l2(img, d["uneven/image"]) <= 1e-4
