@@ -225,6 +225,13 @@ int rtm_server_destroy(rtm_server *server);
 int rtm_server_submit(rtm_server *server, const rtm_params *p, const float *velocity,
                       const float *wavelet, const float *seismogram, long long *request_id);
 /* Admits, runs steps_per_launch batched steps, harvests finished migrations. */
+/* As rtm_server_submit, with the seismogram as a ZFP fixed-accuracy stream of rec_count x nt
+ * (zfp2d_lossyCompression's output, tolerance tol): a host thread of the server decodes it
+ * (rtm_zfp_decode_float2d) while the GPU steps, and the request is admitted once decoded;
+ * a stream that fails to decode makes a later rtm_server_step return RTM_ERR_DECODE. */
+int rtm_server_submit_zfp(rtm_server *server, const rtm_params *p, const float *velocity,
+                          const float *wavelet, const void *zfp_stream, size_t zfp_bytes,
+                          float tol, long long *request_id);
 int rtm_server_step(rtm_server *server, int *n_active, int *n_queued);
 /* One finished migration (RTM_ERR_BUSY if none): image and self image (nx x nz, each may be
  * NULL), times[3] = submit, admission, completion (seconds, monotonic clock; may be NULL). */

@@ -162,6 +162,7 @@ def _declare(L):
         "rtm_server_create": (C.c_int, [C.c_longlong, C.c_int, C.c_int, C.POINTER(vp)]),
         "rtm_server_destroy": (C.c_int, [vp]),
         "rtm_server_submit": (C.c_int, [vp, P, fp, fp, fp, C.POINTER(C.c_longlong)]),
+        "rtm_server_submit_zfp": (C.c_int, [vp, P, fp, fp, vp, C.c_size_t, C.c_float, C.POINTER(C.c_longlong)]),
         "rtm_server_step": (C.c_int, [vp, ip, ip]),
         "rtm_server_poll": (C.c_int, [vp, C.POINTER(C.c_longlong), fp, fp, C.POINTER(C.c_double)]),
         "rtm_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
@@ -193,7 +194,8 @@ def exported_symbols():
             "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_capture_source",
             "rtm_plan_launch_count",
             "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
-            "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_step",
+            "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_submit_zfp",
+            "rtm_server_step",
             "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static",
             "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
             "rtm_zfp_encode_float2d", "rtm_routine_run"]
@@ -453,6 +455,16 @@ class Server:
         q = p.replace()
         _check(lib().rtm_server_submit(self.handle, C.byref(q), _fp(_f32(velocity)), _fp(_f32(wavelet)),
                                        _fp(_f32(seismogram)), C.byref(rid)))
+        self.params[rid.value] = q
+        return rid.value
+
+    def submit_zfp(self, p: RtmParams, velocity, wavelet, stream: bytes, tol: float) -> int:
+        """Submit with the seismogram as a ZFP stream; decoded by the server's host threads."""
+        rid = C.c_longlong()
+        q = p.replace()
+        buf = np.frombuffer(bytes(stream), np.uint8)
+        _check(lib().rtm_server_submit_zfp(self.handle, C.byref(q), _fp(_f32(velocity)), _fp(_f32(wavelet)),
+                                           buf.ctypes.data_as(C.c_void_p), buf.size, C.c_float(tol), C.byref(rid)))
         self.params[rid.value] = q
         return rid.value
 

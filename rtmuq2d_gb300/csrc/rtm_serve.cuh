@@ -17,6 +17,9 @@ struct ServeRequest {
     long long id;
     rtm_params p;
     std::vector<float> vel, wav, seis;     // host copies of the inputs
+    std::vector<unsigned char> zfp;        // ZFP seismogram still to decode (or empty)
+    float zfp_tol = 0.0f;
+    std::atomic<int> ready{1};             // 0 while a decoder thread works on it, -1 failed
     double t_submit, t_admit, t_done;
     std::vector<float> img, slf;
     long long bytes;
@@ -50,6 +53,12 @@ struct rtm_server {
     double busy_ms = 0.0;                  // GPU time of the replays (events)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
+    // host threads decoding ZFP seismograms of submitted requests (rtm_server_submit_zfp)
+    std::vector<std::thread> decoders;
+    std::deque<rtm::ServeRequest *> to_decode;
+    std::mutex dmu;
+    std::condition_variable dcv;
+    bool stopping = false;
 };
 
 namespace rtm {
@@ -267,6 +276,25 @@ static int capture_graph(rtm_server *S)
     return RTM_OK;
 }
 
+static void decoder_loop(rtm_server *S)
+{
+    for (;;) {
+        ServeRequest *R = nullptr;
+        {
+            std::unique_lock<std::mutex> lock(S->dmu);
+            S->dcv.wait(lock, [&] { return S->stopping || !S->to_decode.empty(); });
+            if (S->stopping && S->to_decode.empty()) return;
+            R = S->to_decode.front();
+            S->to_decode.pop_front();
+        }
+        R->seis.resize((size_t)R->p.rec_count * R->p.nt);
+        const int st = rtm_zfp_decode_float2d(R->zfp.data(), R->zfp.size(), (double)R->zfp_tol, R->p.rec_count,
+                                              R->p.nt, R->seis.data());
+        std::vector<unsigned char>().swap(R->zfp);
+        R->ready.store(st == RTM_OK ? 1 : -1);
+    }
+}
+
 }  // namespace rtm
 
 extern "C" {
@@ -306,6 +334,9 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
     RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
     RTM_TRY(capture_graph(S.get()));
     RTM_CUDA(cudaStreamSynchronize(S->stream));
+    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
+    const int nthreads = (int)std::min(8u, hw / 2);
+    for (int k = 0; k < nthreads; ++k) S->decoders.emplace_back(decoder_loop, S.get());
     *out = S.release();
     return RTM_OK;
 }
@@ -313,6 +344,12 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
 int rtm_server_destroy(rtm_server *S)
 {
     if (!S) return RTM_OK;
+    {
+        std::lock_guard<std::mutex> lock(S->dmu);
+        S->stopping = true;
+    }
+    S->dcv.notify_all();
+    for (auto &t : S->decoders) t.join();
     cudaStreamSynchronize(S->stream);
     for (rtm_plan *P : S->slot_plan) if (P) plan_free(P);
     for (rtm_plan *P : S->idle) plan_free(P);
@@ -345,11 +382,34 @@ int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity,
     const size_t nv = (size_t)(p->th_left + p->nx + p->th_right) * (p->th_up + p->nz + p->th_down);
     R->vel.assign(velocity, velocity + nv);
     if (p->n_wavelet > 0) R->wav.assign(wavelet, wavelet + p->n_wavelet);
-    if (p->rec_count > 0) R->seis.assign(seismogram, seismogram + (size_t)p->rec_count * p->nt);
+    if (p->rec_count > 0 && seismogram) R->seis.assign(seismogram, seismogram + (size_t)p->rec_count * p->nt);
     R->bytes = bytes;
     R->t_submit = now_s();
     S->queue.push_back(R);
     if (request_id) *request_id = R->id;
+    return RTM_OK;
+}
+
+// As rtm_server_submit, with the seismogram as a ZFP fixed-accuracy stream (what
+// zfp2d_lossyCompression writes, tolerance `tol`): a host decoder thread decodes it while
+// the GPU steps; the request is admitted once decoded.
+int rtm_server_submit_zfp(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
+                          const void *zfp_stream, size_t zfp_bytes, float tol, long long *request_id)
+{
+    if (!S || !p || !velocity || (!zfp_stream && zfp_bytes)) return fail(RTM_ERR_INVALID, "null argument");
+    long long id = 0;
+    RTM_TRY(rtm_server_submit(S, p, velocity, wavelet, nullptr, &id));
+    ServeRequest *R = S->queue.back();
+    R->zfp.assign(static_cast<const unsigned char *>(zfp_stream),
+                  static_cast<const unsigned char *>(zfp_stream) + zfp_bytes);
+    R->zfp_tol = tol;
+    R->ready.store(0);
+    {
+        std::lock_guard<std::mutex> lock(S->dmu);
+        S->to_decode.push_back(R);
+    }
+    S->dcv.notify_one();
+    if (request_id) *request_id = id;
     return RTM_OK;
 }
 
@@ -358,9 +418,18 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
 {
     if (!S) return fail(RTM_ERR_INVALID, "null server");
     bool changed = false;
-    // admission in arrival order (head of line blocks: requests are served FIFO)
-    while (!S->queue.empty()) {
-        ServeRequest *R = S->queue.front();
+    // admission in arrival order among the requests whose inputs are ready (a request whose
+    // seismogram is still being decoded is passed over; one that does not fit blocks the rest)
+    for (auto it = S->queue.begin(); it != S->queue.end();) {
+        ServeRequest *R = *it;
+        const int ready = R->ready.load();
+        if (ready == 0) { ++it; continue; }
+        if (ready < 0) {
+            const long long rid = R->id;
+            S->queue.erase(it);
+            delete R;
+            return fail(RTM_ERR_DECODE, "request %lld: the ZFP seismogram could not be decoded", rid);
+        }
         int slot = -1;
         for (int m = 0; m < S->max_members; ++m)
             if (!S->slot_plan[m]) { slot = m; break; }
@@ -372,7 +441,7 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
         if (!reusable && S->in_use - idle_bytes + R->bytes > S->budget) break;
         const int st = admit(S, slot, R);
         if (st != RTM_OK) return st;
-        S->queue.pop_front();
+        it = S->queue.erase(it);
         changed = true;
     }
     if (changed) {

@@ -125,14 +125,18 @@ def serving_template(k: int, nt: int = 7500) -> tuple:
     return p, true, mig
 
 
+SERVING_NT = (2000, 3000, 4000, 5000, 6000, 7500)
+
+
 def serving_trace(n: int, seed: int = 23):
     """Requests of the serving trace: grid template uniform over SERVING_GRIDS, nt uniform
-    in [2000, 7500], FP32 or BF16 ring storage, own realization seed."""
+    over SERVING_NT (2000..7500; a few values so that each (grid, nt) seismogram is
+    ZFP-compressed once), FP32 or BF16 ring storage, own realization seed."""
     rng = np.random.default_rng(seed)
     reqs = []
     for i in range(n):
         reqs.append({"grid": int(rng.integers(0, len(SERVING_GRIDS))),
-                     "nt": int(rng.integers(100, 376)) * 20,    # 2000..7500, whole slices
+                     "nt": int(SERVING_NT[int(rng.integers(0, len(SERVING_NT)))]),
                      "precision": int(rng.integers(0, 2)),
                      "seed": seed * 100000 + i})
     return reqs

@@ -112,3 +112,20 @@ def _valid(engine, p):
         return True
     except engine.RtmError:
         return False
+
+
+def test_server_zfp_submission_equals_decoded_submission(engine):
+    """A request carrying the ZFP stream (decoded by the server's host threads while the GPU
+    steps) gives the image of the same request carrying the decoded seismogram."""
+    d = load()
+    p, ext, wav, _ = _case(engine, d, "uneven", storage=1)
+    stream = d["zfp/tol1e-4/stream"].tobytes()
+    decoded = d["zfp/tol1e-4/decoded"]
+    ref = _alone(engine, (p, ext, wav, decoded))[0]
+    srv = engine.Server(0, max_members=4, steps_per_launch=16)
+    rid = srv.submit_zfp(p, ext, wav, stream, 1e-4)
+    rid2 = srv.submit(p, ext, wav, decoded)
+    out = srv.run_all()
+    srv.close()
+    assert np.array_equal(out[rid][0], ref)
+    assert np.array_equal(out[rid2][0], ref)
