@@ -123,24 +123,37 @@ __device__ __forceinline__ void margs(const BMember<T> &M, int t, int role, MArg
 // (absorbingBoundaryCondition.c:191-217 left, 237-263 top, 283-310 right, 330-357 bottom);
 // same arithmetic as cpml_x_quad / cpml_z_quad (rtm_step.cuh).  c4 gets the correction.
 template <typename T>
-__device__ __forceinline__ void strip_x_quad(const T *psi, T *xi, size_t P, T ab, T bb, const T (&W)[9][4],
+__device__ __forceinline__ void strip_x_quad(const T *psi, T *xi, const T *ucol, size_t P, T ab, T bb,
                                              const T (&cf)[4], int zq, int zlo, int zhi, T h1, T h2, T h3,
                                              bool fresh, T (&c4)[4])
 {
-    T acc[4];
+    // dpsi (B coefficients) and D2 along x (AC coefficients) accumulated one row pair at a
+    // time, +-4 first, in the operand order of cpml_x_quad / d2x_w, so that only two rows of
+    // each field are live at once
+    T acc[4], d2[4];
     {
         const T bk[4] = {(T)RTM_B4, (T)RTM_B3, (T)RTM_B2, (T)RTM_B1};
+        const T ak[4] = {(T)RTM_AC4, (T)RTM_AC3, (T)RTM_AC2, (T)RTM_AC1};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            T mk[4], pk[4];
-            ld4(psi - (ptrdiff_t)(4 - k) * (ptrdiff_t)P, mk);
-            ld4(psi + (ptrdiff_t)(4 - k) * (ptrdiff_t)P, pk);
+            const ptrdiff_t off = (ptrdiff_t)(4 - k) * (ptrdiff_t)P;
+            T mk[4], pk[4], um[4], up[4];
+            ld4(psi - off, mk);
+            ld4(psi + off, pk);
+            ld4(ucol - off, um);
+            ld4(ucol + off, up);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const T term = bk[k] * (pk[j] - mk[j]);
                 acc[j] = k == 0 ? term : acc[j] + term;
+                const T dterm = ak[k] * (up[j] + um[j]);
+                d2[j] = k == 0 ? dterm : d2[j] + dterm;
             }
         }
+        T uc[4];
+        ld4(ucol, uc);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d2[j] = d2[j] + (T)RTM_AC0 * uc[j];
     }
     T x4[4];
     if (fresh) {
@@ -155,7 +168,7 @@ __device__ __forceinline__ void strip_x_quad(const T *psi, T *xi, size_t P, T ab
         c4[j] = (T)0;
         if (z >= zlo && z < zhi) {
             const T dp = acc[j] * h1;
-            const T xn = bb * x4[j] + ab * (d2x_w<T>(W, j) * h3 + dp);
+            const T xn = bb * x4[j] + ab * (d2[j] * h3 + dp);
             x4[j] = xn;
             c4[j] = (cf[j] * h2) * (dp + xn);
         }
@@ -286,19 +299,14 @@ __device__ __forceinline__ bool strip_quad(const BMember<T> &M, const CorrShape 
     ld4(M.coef + (size_t)x * P + zq, cf);
     ld4(un + (size_t)x * P + zq, fv);
     const T *col = u + (size_t)x * P + zq;
-    if (inL || inR) {
-        T W[9][4];
-#pragma unroll
-        for (int m = 0; m < 9; ++m) ld4(col + (ptrdiff_t)(m - 4) * (ptrdiff_t)P, W[m]);
-        if (inL)
-            strip_x_quad<T>(M.psi[0] + (size_t)x * P + zq, M.xi[0] + (size_t)x * P + zq, P, (T)M.prof[0][x],
-                            (T)M.prof[1][x], W, cf, zq, 4, g.dimz - 4, M.h1, M.h2, M.h3, fresh, cx);
-        else {
-            const int li = x - (g.dimx - g.thr);
-            strip_x_quad<T>(M.psi[1] + (size_t)li * P + zq, M.xi[1] + (size_t)li * P + zq, P,
-                            (T)M.prof[2][li], (T)M.prof[3][li], W, cf, zq, 4, g.dimz - 4, M.h1, M.h2,
-                            M.h3, fresh, cx);
-        }
+    if (inL)
+        strip_x_quad<T>(M.psi[0] + (size_t)x * P + zq, M.xi[0] + (size_t)x * P + zq, col, P, (T)M.prof[0][x],
+                        (T)M.prof[1][x], cf, zq, 4, g.dimz - 4, M.h1, M.h2, M.h3, fresh, cx);
+    else if (inR) {
+        const int li = x - (g.dimx - g.thr);
+        strip_x_quad<T>(M.psi[1] + (size_t)li * P + zq, M.xi[1] + (size_t)li * P + zq, col, P,
+                        (T)M.prof[2][li], (T)M.prof[3][li], cf, zq, 4, g.dimz - 4, M.h1, M.h2, M.h3,
+                        fresh, cx);
     }
     if (inT || inB) {
         T c4[4], zz[12];
