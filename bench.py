@@ -73,6 +73,23 @@ def dist_env():
     return ws, rank, local
 
 
+def shard(items, rank, world):
+    """Round-robin share of independent units (migrations) for one rank: the path shards by
+    migration, with no exchange between ranks."""
+    return list(items[rank::world])
+
+
+def reduce_over_ranks(x, op, ws, device):
+    """max or sum of a float over the ranks of the default process group (x itself at ws 1)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def workload(args, with_seis=True):
     """Params and seeded host inputs of the benchmarked workload."""
     from rtmuq2d_gb300 import workloads
@@ -226,13 +243,16 @@ def cpu_sample(p, ext, wav, seis, target_s, dtype=np.float32):
                       "(oracle/rtm_oracle.c, -O3 OpenMP)" % (p.dim_x, p.dim_z, nt, p.nt)}
 
 
-def run_batched(args, eng):
+def run_batched(args, eng, rank=0, ws=1):
     """The batched UQ ensemble through the serving engine: every member resident at once,
     advanced together by the batched step kernels.  Timed from the first submit (host
     buffers) to the last image on the host; a sample of the members is also run one at a
-    time through the plain path for the served-vs-plain ratio."""
+    time through the plain path for the served-vs-plain ratio.  With N ranks each runs its
+    round-robin share of the members; value = all ranks' cell-updates / the slowest rank's
+    time."""
     from rtmuq2d_gb300 import workloads
     members, true, mig = workloads.ensemble(args.batch_members, args.batch_nt)
+    members = shard(members, rank, ws)
     wav = workloads.wavelet_for(members[0]["params"])
     inputs = []
     for m in members:
@@ -289,12 +309,16 @@ def run_batched(args, eng):
                      "note": "CUDA events around graph replays of the server's stream"}
     agree = max((float(np.linalg.norm(out[ids[i]][0] - img) / max(np.linalg.norm(img), 1e-30))
                  for i, img in plain_images.items()), default=None)
+    local_cells = cells
+    cells = reduce_over_ranks(local_cells, "sum", ws, "cuda")
+    wall = reduce_over_ranks(wall, "max", ws, "cuda")
     widths = [p.nx for p, *_ in inputs]
     value = cells / wall / 1e9
-    return {"workload": "uq_ensemble_%dx_windows%d-%d_nz700_nt%d" % (len(inputs), min(widths),
+    n_members = int(reduce_over_ranks(len(inputs), "sum", ws, "cuda"))
+    return {"workload": "uq_ensemble_%dx_windows%d-%d_nz700_nt%d" % (n_members, min(widths),
                                                                       max(widths), args.batch_nt),
-            "members": len(inputs), "value": value, "unit": "Gcell-updates/s",
-            "seconds": wall, "gpu_busy_value": cells / (st["gpu_ms"] * 1e-3) / 1e9,
+            "members": n_members, "ranks": ws, "value": value, "unit": "Gcell-updates/s",
+            "seconds": wall, "gpu_busy_value": local_cells / (st["gpu_ms"] * 1e-3) / 1e9,
             "plain_value_same_members": plain, "plain_sample": len(sample),
             "speedup_vs_plain": value / plain if plain else None,
             "image_agreement_with_plain_rel_l2": agree,
@@ -536,12 +560,7 @@ def run_gpu(args):
     prof = plan.profile_read()
     plan.profile(0)
     launches = plan.launches - launches0
-    total_ms = float(sum(times))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_over_ranks(float(sum(times)), "max", ws, "cuda")
     cells = p.cell_updates
     value = ws * args.steps * cells / (total_ms * 1e-3) / 1e9
     if args.quick:
@@ -565,16 +584,19 @@ def run_gpu(args):
         dt = (time.perf_counter() - t0) * 1e3
         if i > 0:
             e2e_ms.append(dt)
-    e2e_total = float(sum(e2e_ms))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = reduce_over_ranks(float(sum(e2e_ms)), "max", ws, "cuda")
     e2e_value = ws * args.steps * cells / (e2e_total * 1e-3) / 1e9
     # sanity: the device-resident and host paths produce the same image
     dev_img = d_img.cpu().numpy()
     agree = float(np.linalg.norm(dev_img - img_h) / max(np.linalg.norm(img_h), 1e-30))
+
+    # batched UQ ensemble: every rank runs its share of the members (sharded by migration)
+    batched = None
+    if args.batch_members > 0:
+        barrier()
+        with ClockSampler(local) as smp:
+            batched = run_batched(args, eng, rank, ws)
+        batched["clocks"] = smp.summary()
 
     if rank != 0:
         if ws > 1:
@@ -596,11 +618,7 @@ def run_gpu(args):
                 "fwd_kernel_achieved_gbs": nbytes["k_step_fwd"] / (fwd_avg_ms * 1e-3) / 1e9,
                 "note": "fields stream from HBM every step (warm-cache ncu: 37 MB read per "
                         "forward step, L2 hit rate 47%); traffic: cold-cache ncu reads"}
-    batched = served = None
-    if ws == 1 and args.batch_members > 0:
-        with ClockSampler(local) as smp:
-            batched = run_batched(args, eng)
-        batched["clocks"] = smp.summary()
+    served = None
     if ws == 1 and args.serve_requests > 0:
         cap = batched["value"] if batched else value
         with ClockSampler(local) as smp:
