@@ -449,6 +449,7 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
                 else if (st.x == 2 && st.y > nt) { st.x = 3; st.y = 0; }
                 state[k] = st;
             }
+            done[2] = 0u;                              // k_mstep's chunk counter
             atomicExch(done, 0u);
             __threadfence();
         }
@@ -491,10 +492,11 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
 // One batched step: every tile of every active member, in two phases (BatchIndex): phase 1
 // = each member's interior field tiles (tile_coords order nb..tiles-1) and, backward with
 // ring storage, its source-field tiles; phase 2 = each member's field tiles touching a CPML
-// strip (tile_coords order 0..nb-1).  Items go to CTAs in chunks of kChunk consecutive items
-// (chunk c to CTA c mod G), so that consecutive items of a CTA mostly share their member and
-// role; an NS-stage TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi
-// of the same step runs alongside, and k_bstrip completes the strip cells afterwards.
+// strip (tile_coords order 0..nb-1).  Items go to CTAs in chunks of kChunk consecutive items,
+// so that consecutive items of a CTA mostly share their member and role; a CTA's first chunk
+// is its index, the later ones come from a step-wide counter (dynamic balance).  An NS-stage
+// TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi of the same step
+// runs alongside, and k_bstrip completes the strip cells afterwards.
 constexpr int kChunk = 4;
 
 template <typename T>
@@ -539,11 +541,19 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
     // Thread 0 maps the i-th work item of this CTA to (member, role, tile), builds the
     // arguments of (member, role) when they differ from the last item's (in the argument
     // slot the other stage is not using) and starts the stage's TMA loads.
+    // Chunk k of this CTA: chunk blockIdx.x first, then the next chunk of the step's counter
+    // (done[2]), fetched one chunk ahead so that the atomic's latency hides behind the
+    // chunk's items.  A CTA's chunks only grow, so its items stay in work-list order.
     int cur1 = 0, cur2 = 0;              // member of the latest item of each phase (monotone)
     int last_key = -1, last_args = 0;
     int l_mu = 0, l_mp = 0;
+    int chunk = blockIdx.x, ahead = 0x0fffffff;   // (past every work list)
     auto issue = [&](int i, int s) {
-        const int tg = (blockIdx.x + (i / kChunk) * gridDim.x) * kChunk + i % kChunk;
+        if (i % kChunk == 0) {
+            if (i > 0) chunk = ahead;
+            if (chunk * kChunk < total) ahead = (int)atomicAdd(done + 2, 1u) + (int)gridDim.x;
+        }
+        const int tg = chunk * kChunk + i % kChunk;
         if (tg >= total) {
             // past the end: the chunk index only grows, so every later item is too
             tile_of[s] = -1;

@@ -191,7 +191,9 @@ struct PsiArgs {
 // ---- batched steps (rtm_batch.cuh) -------------------------------------------------------
 // state[m] = (pass, step): pass 0 idle, 1 forward (nt steps), 2 backward (nt + 1 steps,
 // the last one images only), 3 finished.
-// done[0]: CTA counter of the step in flight (zero between launches); done[1]: error bits.
+// done[0]: CTA counter of the step in flight (zero between launches); done[1]: error bits;
+// done[2]: chunk counter of k_mstep (cleared by k_bstrip's last CTA).
+constexpr int kBatchDoneWords = 3;
 template <typename T>
 cudaError_t launch_bpsi(const BatchIndex *ix, const BMember<T> *mem, const int2 *state, int grid,
                         int pdl, cudaStream_t s);

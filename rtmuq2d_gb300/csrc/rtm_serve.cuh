@@ -320,10 +320,10 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
     RTM_CUDA(cudaMalloc(&S->d_ix, sizeof(BatchIndex)));
     RTM_CUDA(cudaMalloc(&S->d_mem, sizeof(BMember<float>) * kMaxMembers));
     RTM_CUDA(cudaMalloc(&S->d_state, sizeof(int2) * kMaxMembers));
-    RTM_CUDA(cudaMalloc(&S->d_done, 2 * sizeof(unsigned)));
+    RTM_CUDA(cudaMalloc(&S->d_done, kBatchDoneWords * sizeof(unsigned)));
     RTM_CUDA(cudaMallocHost(&S->h_state, sizeof(int2) * kMaxMembers));
     RTM_CUDA(cudaMemsetAsync(S->d_state, 0, sizeof(int2) * kMaxMembers, S->stream));
-    RTM_CUDA(cudaMemsetAsync(S->d_done, 0, 2 * sizeof(unsigned), S->stream));
+    RTM_CUDA(cudaMemsetAsync(S->d_done, 0, kBatchDoneWords * sizeof(unsigned), S->stream));
     RTM_CUDA(cudaEventCreate(&S->ev0));
     RTM_CUDA(cudaEventCreate(&S->ev1));
     S->mem.resize(kMaxMembers);

@@ -129,3 +129,44 @@ def test_server_zfp_submission_equals_decoded_submission(engine):
     srv.close()
     assert np.array_equal(out[rid][0], ref)
     assert np.array_equal(out[rid2][0], ref)
+
+
+def _phase_cases(engine, oracle):
+    """Grids large enough to hold interior tiles (phase 1 of the batched step) beside tiles
+    touching a CPML strip (phase 2): the 400 x 200 workload, and a 250 x 258 grid with CPML 30
+    whose last z-tile row is shorter than the bottom CPML band."""
+    from rtmuq2d_gb300 import workloads
+    p = workloads.params_small()
+    true, mig = workloads.models_small(p, seed=0)
+    wav = workloads.wavelet_for(p)
+    ext = engine.extend_matrix(p, mig)
+    seis = oracle.model_seismogram(p.as_dict(), engine.extend_matrix(p, true), wav)
+    q = workloads.params_small(nx=250, nz=258, th_left=30, th_right=30, th_up=30, th_down=30,
+                               nt=1200, shot_x=125, rec_count=125)
+    tq, mq = workloads.models_small(q, seed=3)
+    wq = workloads.wavelet_for(q)
+    extq = engine.extend_matrix(q, mq)
+    seisq = oracle.model_seismogram(q.as_dict(), engine.extend_matrix(q, tq), wq)
+    return [(p.replace(storage=1), ext, wav, seis),
+            (q.replace(storage=1), extq, wq, seisq),
+            (p.replace(storage=0), ext, wav, seis),
+            (q.replace(storage=0, nt=600), extq, wq, np.ascontiguousarray(seisq[:, :600]))]
+
+
+def test_server_clear_and_strip_tiles_match_plain_and_oracle(engine, oracle):
+    cases = _phase_cases(engine, oracle)
+    assert all(_valid(engine, c[0]) for c in cases)
+    # two slots for four members of two grids and three time axes: members in different
+    # passes share every batched step
+    srv = engine.Server(0, max_members=2, steps_per_launch=16)
+    ids = [srv.submit(*c) for c in cases]
+    out = srv.run_all()
+    srv.close()
+    for rid, c in zip(ids, cases):
+        img, slf = engine.migrate_shot(*c)
+        assert rel_l2(out[rid][0], img) <= 1e-5, rid
+        assert rel_l2(out[rid][1], slf) <= 1e-5, rid
+    for rid, c in zip(ids[:2], cases[:2]):
+        ref_img, ref_slf = oracle.migrate(c[0].as_dict(), c[1], c[2], c[3])
+        assert rel_l2(out[rid][0], ref_img) <= 1e-4, rid
+        assert rel_l2(out[rid][1], ref_slf) <= 1e-4, rid
