@@ -239,6 +239,11 @@ int rtm_server_poll(rtm_server *server, long long *request_id, float *image, flo
                     double *times);
 int rtm_server_stats(const rtm_server *server, long long *cell_updates, double *gpu_ms,
                      long long *launches, long long *bytes_in_use);
+/* CUDA-event time (ms) of the batched tile kernel on the second time step of the last
+ * rtm_server_step's graph replay, launched without overlapping the kernels around it
+ * (steps_per_launch >= 2; 0 otherwise).  For the kernel's roofline; the step itself
+ * advances every active member as usual. */
+int rtm_server_kernel_ms(const rtm_server *server, double *tile_kernel_ms);
 
 /* ---- migration without device allocation -------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc: a host whose

@@ -167,6 +167,7 @@ def _declare(L):
         "rtm_server_poll": (C.c_int, [vp, C.POINTER(C.c_longlong), fp, fp, C.POINTER(C.c_double)]),
         "rtm_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "rtm_server_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double)]),
         "rtm_migrate_shot_static": (C.c_int, [P, vp, vp, vp, vp, vp, vp]),
         "rtm_zfp_decode_float2d": (C.c_int, [vp, C.c_size_t, C.c_double, C.c_int, C.c_int, fp]),
         "rtm_zfp_decode_file": (C.c_int, [C.c_char_p, fp, C.c_int, C.c_int, C.c_float]),
@@ -196,7 +197,7 @@ def exported_symbols():
             "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
             "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_submit_zfp",
             "rtm_server_step",
-            "rtm_server_poll", "rtm_server_stats", "rtm_migrate_shot_static",
+            "rtm_server_poll", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
             "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
             "rtm_zfp_encode_float2d", "rtm_routine_run"]
 
@@ -496,6 +497,13 @@ class Server:
         cu, ms, ln, by = C.c_longlong(), C.c_double(), C.c_longlong(), C.c_longlong()
         _check(lib().rtm_server_stats(self.handle, C.byref(cu), C.byref(ms), C.byref(ln), C.byref(by)))
         return {"cell_updates": cu.value, "gpu_ms": ms.value, "launches": ln.value, "bytes_in_use": by.value}
+
+    def kernel_ms(self) -> float:
+        """CUDA-event time of the tile kernel on the second step of the last step() call's
+        graph replay (launched without overlap; 0 if steps_per_launch < 2)."""
+        v = C.c_double()
+        _check(lib().rtm_server_kernel_ms(self.handle, C.byref(v)))
+        return v.value
 
     def run_all(self):
         """Steps until every submitted migration has finished; returns {id: (img, self, times)}."""

@@ -494,10 +494,11 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
 // ring storage, its source-field tiles; phase 2 = each member's field tiles touching a CPML
 // strip (tile_coords order 0..nb-1).  Items go to CTAs in chunks of kChunk consecutive items,
 // so that consecutive items of a CTA mostly share their member and role; a CTA's first chunk
-// is its index, the later ones come from a step-wide counter (dynamic balance).  An NS-stage
-// TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi of the same step
+// is its index, the later ones come from a step-wide counter (dynamic balance, single items
+// in the tail).  An NS-stage TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi of the same step
 // runs alongside, and k_bstrip completes the strip cells afterwards.
 constexpr int kChunk = 4;
+constexpr int kTail = 2;                  // single-item grabs for the last kTail * G items
 
 template <typename T>
 __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
@@ -541,19 +542,30 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
     // Thread 0 maps the i-th work item of this CTA to (member, role, tile), builds the
     // arguments of (member, role) when they differ from the last item's (in the argument
     // slot the other stage is not using) and starts the stage's TMA loads.
-    // Chunk k of this CTA: chunk blockIdx.x first, then the next chunk of the step's counter
-    // (done[2]), fetched one chunk ahead so that the atomic's latency hides behind the
-    // chunk's items.  A CTA's chunks only grow, so its items stay in work-list order.
+    // Items [pos, end) of this CTA: kChunk items at blockIdx.x * kChunk first, then grabs
+    // from the step's counter (done[2], items past the G * kChunk static ones): kChunk items
+    // while more than kTail * G remain, single items in the tail, so that CTAs finish
+    // together.  The next grab is fetched one grab ahead so that the atomic's latency hides
+    // behind the items; a CTA's grabs only grow, so its items stay in work-list order.
     int cur1 = 0, cur2 = 0;              // member of the latest item of each phase (monotone)
     int last_key = -1, last_args = 0;
     int l_mu = 0, l_mp = 0;
-    int chunk = blockIdx.x, ahead = 0x0fffffff;   // (past every work list)
+    const int base = (int)gridDim.x * kChunk;
+    int pos = blockIdx.x * kChunk, end = pos + kChunk;
+    int ahead = 0x0fffffff, ahead_n = 1;  // (past every work list)
+    auto grab = [&](int seen) {           // seen: the latest position this CTA knows of
+        ahead_n = seen < total - kTail * (int)gridDim.x ? kChunk : 1;
+        ahead = base + (int)atomicAdd(done + 2, (unsigned)ahead_n);
+    };
     auto issue = [&](int i, int s) {
-        if (i % kChunk == 0) {
-            if (i > 0) chunk = ahead;
-            if (chunk * kChunk < total) ahead = (int)atomicAdd(done + 2, 1u) + (int)gridDim.x;
+        if (i == 0) {
+            if (pos < total) grab(pos);
+        } else if (pos >= end) {
+            pos = ahead;
+            end = ahead + ahead_n;
+            if (pos < total) grab(pos);
         }
-        const int tg = chunk * kChunk + i % kChunk;
+        const int tg = pos++;
         if (tg >= total) {
             // past the end: the chunk index only grows, so every later item is too
             tile_of[s] = -1;

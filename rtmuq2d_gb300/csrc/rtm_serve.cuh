@@ -52,6 +52,11 @@ struct rtm_server {
     long long launches = 0;
     double busy_ms = 0.0;                  // GPU time of the replays (events)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the tile kernel of the second step of each replay, timed alone (no overlap with the
+    // kernels around it): events recorded by the graph, read after each replay
+    cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+    bool kernel_sampled = false;
+    double kernel_ms_last = 0.0;
     std::string err;
     // host threads decoding ZFP seismograms of submitted requests (rtm_server_submit_zfp)
     std::vector<std::thread> decoders;
@@ -254,11 +259,16 @@ static int capture_graph(rtm_server *S)
     const int pgrid = 4 * sms;
     RTM_CUDA(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
+    S->kernel_sampled = S->steps_per_launch >= 2;
     for (int k = 0; k < S->steps_per_launch && e == cudaSuccess; ++k) {
+        const bool sample = S->kernel_sampled && k == 1;
         e = launch_bpsi<float>(S->d_ix, S->d_mem, S->d_state, pgrid, k > 0, S->stream);
-        if (e == cudaSuccess) e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, 1, S->stream);
+        if (e == cudaSuccess && sample) e = cudaEventRecordWithFlags(S->kev0, S->stream, cudaEventRecordExternal);
         if (e == cudaSuccess)
-            e = launch_bstrip<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, pgrid, 1, S->stream);
+            e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, !sample, S->stream);
+        if (e == cudaSuccess && sample) e = cudaEventRecordWithFlags(S->kev1, S->stream, cudaEventRecordExternal);
+        if (e == cudaSuccess)
+            e = launch_bstrip<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, pgrid, !sample, S->stream);
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(S->stream, &graph);
@@ -326,6 +336,8 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
     RTM_CUDA(cudaMemsetAsync(S->d_done, 0, kBatchDoneWords * sizeof(unsigned), S->stream));
     RTM_CUDA(cudaEventCreate(&S->ev0));
     RTM_CUDA(cudaEventCreate(&S->ev1));
+    RTM_CUDA(cudaEventCreate(&S->kev0));
+    RTM_CUDA(cudaEventCreate(&S->kev1));
     S->mem.resize(kMaxMembers);
     S->slot_plan.assign(max_members, nullptr);
     S->slot_req.assign(max_members, nullptr);
@@ -360,6 +372,7 @@ int rtm_server_destroy(rtm_server *S)
     cudaFree(S->d_ix); cudaFree(S->d_mem); cudaFree(S->d_state); cudaFree(S->d_done);
     cudaFreeHost(S->h_state);
     cudaEventDestroy(S->ev0); cudaEventDestroy(S->ev1);
+    cudaEventDestroy(S->kev0); cudaEventDestroy(S->kev1);
     cudaStreamDestroy(S->stream);
     delete S;
     return RTM_OK;
@@ -461,6 +474,11 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
         float ms = 0.0f;
         RTM_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
         S->busy_ms += ms;
+        if (S->kernel_sampled) {
+            float kms = 0.0f;
+            RTM_CUDA(cudaEventElapsedTime(&kms, S->kev0, S->kev1));
+            S->kernel_ms_last = kms;
+        }
         unsigned flags[2] = {0, 0};
         RTM_CUDA(cudaMemcpy(flags, S->d_done, sizeof flags, cudaMemcpyDeviceToHost));
         if (flags[1]) return fail(RTM_ERR_TIMEOUT, "a batched tile load timed out");
@@ -513,6 +531,13 @@ int rtm_server_stats(const rtm_server *S, long long *cell_updates, double *gpu_m
     if (gpu_ms) *gpu_ms = S->busy_ms;
     if (launches) *launches = S->launches;
     if (bytes_in_use) *bytes_in_use = S->in_use;
+    return RTM_OK;
+}
+
+int rtm_server_kernel_ms(const rtm_server *S, double *tile_kernel_ms)
+{
+    if (!S || !tile_kernel_ms) return fail(RTM_ERR_INVALID, "null argument");
+    *tile_kernel_ms = S->kernel_sampled ? S->kernel_ms_last : 0.0;
     return RTM_OK;
 }
 
