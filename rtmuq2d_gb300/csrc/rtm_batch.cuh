@@ -355,6 +355,12 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
     __shared__ int s_base[kMaxMembers + 1];
     __shared__ int2 s_state[kMaxMembers];
     __shared__ float red[kStripBlock / 32];
+    // The current member's descriptor (all but its tensor maps), staged by one coalesced
+    // copy per member change, so that an item's addresses come from shared memory and its
+    // data loads all issue at once.
+    constexpr int kMapBytes = (int)offsetof(BMember<T>, g);
+    static_assert(kMapBytes % 16 == 0 && sizeof(BMember<T>) % 16 == 0, "16-byte copy of the descriptor");
+    __shared__ __align__(64) int4 s_desc[sizeof(BMember<T>) / 16];
     // the next step's k_bpsi may launch; it waits for this grid to complete
     griddep_launch();
     const int nmem = ix->nmem;
@@ -363,11 +369,19 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
     griddep_wait();                                    // this step's tiles (and psi)
     __syncthreads();
     const int n = s_base[nmem];
-    int m = 0;
+    int m = 0, m_desc = -1;
     for (int base = blockIdx.x * kStripBlock; base < n; base += gridDim.x * kStripBlock) {
         while (s_base[m + 1] <= base) ++m;             // block-uniform member
+        if (m != m_desc) {
+            __syncthreads();                           // the previous member's items are done
+            const int4 *src = reinterpret_cast<const int4 *>(mem + m);
+            for (int k = kMapBytes / 16 + threadIdx.x; k < (int)(sizeof(BMember<T>) / 16); k += blockDim.x)
+                s_desc[k] = src[k];
+            __syncthreads();
+            m_desc = m;
+        }
         const int2 st = s_state[m];
-        const BMember<T> &M = mem[m];
+        const BMember<T> &M = *reinterpret_cast<const BMember<T> *>(s_desc);
         const Geom &g = M.g;
         const bool live = (st.x == 1 || st.x == 2) && st.y < g.nt;
         const CorrShape cs = corr_shape(g);
