@@ -15,6 +15,11 @@ static_assert(alignof(BMember<float>) >= 64 && sizeof(BMember<float>) % 64 == 0,
               "tensor maps of consecutive members must stay 64-byte aligned");
 
 // Orders the host's earlier writes of a tensor map in global memory before its use by TMA.
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m)
 {
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
@@ -295,6 +300,37 @@ __device__ __forceinline__ bool strip_quad(const BMember<T> &M, const CorrShape 
     const bool inT = zq + 4 > 4 && zq < g.thu - 4;                 // every column (the quirk)
     const bool inB = x >= 4 && x < g.dimx - 4 && zq + 4 > g.dimz - g.thd + 4 && zq < g.dimz - 4;
     if (!(inL || inR || inT || inB)) return false;
+    // Request every line of the item at once (no registers held); the loads below, which
+    // the register budget issues a few at a time, then mostly find them in L2.
+    {
+        const T *col = u + (size_t)x * P + zq;
+        prefetch_l2(M.coef + (size_t)x * P + zq);
+        prefetch_l2(un + (size_t)x * P + zq);
+        prefetch_l2(col - 4);
+        prefetch_l2(col + 4);
+        if (inL || inR) {
+            const T *ps = inL ? M.psi[0] + (size_t)x * P + zq
+                              : M.psi[1] + (size_t)(x - (g.dimx - g.thr)) * P + zq;
+#pragma unroll
+            for (int k = 1; k <= 4; ++k) {
+                prefetch_l2(ps - (ptrdiff_t)k * (ptrdiff_t)P);
+                prefetch_l2(ps + (ptrdiff_t)k * (ptrdiff_t)P);
+                prefetch_l2(col - (ptrdiff_t)k * (ptrdiff_t)P);
+                prefetch_l2(col + (ptrdiff_t)k * (ptrdiff_t)P);
+            }
+            prefetch_l2((inL ? M.xi[0] + (size_t)x * P : M.xi[1] + (size_t)(x - (g.dimx - g.thr)) * P) + zq);
+        }
+        if (inT) {
+            prefetch_l2(M.psi[2] + (size_t)x * g.st + zq - 4);
+            prefetch_l2(M.psi[2] + (size_t)x * g.st + zq + 4);
+            prefetch_l2(M.xi[2] + (size_t)x * g.st + zq);
+        } else if (inB) {
+            const int lq = zq - g.zb0;
+            prefetch_l2(M.psi[3] + (size_t)x * g.sb + lq - 4);
+            prefetch_l2(M.psi[3] + (size_t)x * g.sb + lq + 4);
+            prefetch_l2(M.xi[3] + (size_t)x * g.sb + lq);
+        }
+    }
     T cf[4], cx[4], cz[4];
     ld4(M.coef + (size_t)x * P + zq, cf);
     ld4(un + (size_t)x * P + zq, fv);

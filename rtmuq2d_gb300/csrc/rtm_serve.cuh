@@ -32,6 +32,12 @@ struct rtm_server {
     int max_members = rtm::kMaxMembers;
     int steps_per_launch = 16;
     cudaStream_t stream = nullptr;
+    // admission uploads run on their own stream while the graph replays on `stream`; the
+    // admitted members are activated (descriptor, state) on `stream` after both
+    cudaStream_t up = nullptr;
+    cudaEvent_t up_ev = nullptr;
+    std::vector<int> pending;              // slots uploaded, not yet activated
+    double last_replay_ms = 0.0;
     // device side
     rtm::BatchIndex *d_ix = nullptr;
     rtm::BMember<float> *d_mem = nullptr;
@@ -152,7 +158,10 @@ static void rebuild_index(rtm_server *S)
     S->ix.corr_base[S->max_members] = cb;
 }
 
-// Sets up one admitted request in slot m on the server's stream.
+// Uploads one admitted request into slot m on the upload stream: the graph replaying on the
+// server's stream touches only active members, and this one becomes active (activate) after
+// the replay and these uploads.  The sources are the request's pageable host copies: each
+// copy returns once its data is staged, so they are released right after.
 static int admit(rtm_server *S, int m, ServeRequest *R)
 {
     rtm_plan *P = nullptr;
@@ -179,21 +188,15 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
     const Geom &g = P->g;
     if (g.tx != kBatchTileX)              // tensor-map boxes must match the kernel's tiles
         return fail(RTM_ERR_INVALID, "batched member with tile width %d (needs %d)", g.tx, kBatchTileX);
-    cudaStream_t s = S->stream;
+    cudaStream_t s = S->up;
     float *stage = P->at<float>(P->L.staging);
-    float *h;
-    RTM_TRY(pinned(P, std::max(R->vel.size(), R->seis.size()) * sizeof(float), &h));
-    RTM_CUDA(cudaStreamSynchronize(s));
-    memcpy(h, R->vel.data(), R->vel.size() * sizeof(float));
-    RTM_CUDA(cudaMemcpyAsync(stage, h, R->vel.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    RTM_CUDA(cudaMemcpyAsync(stage, R->vel.data(), R->vel.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     RTM_CUDA(launch_coef<float>(g, stage, g.dimz, P->at<float>(P->L.coef), P->p.dx, P->p.dt, s));
     if (g.nwav > 0)
         RTM_CUDA(cudaMemcpyAsync(P->at<float>(P->L.wav), R->wav.data(), sizeof(float) * g.nwav,
                                  cudaMemcpyHostToDevice, s));
-    if (g.nrec > 0) {
-        RTM_CUDA(cudaStreamSynchronize(s));     // staging and the pinned buffer are reused
-        memcpy(h, R->seis.data(), R->seis.size() * sizeof(float));
-        RTM_CUDA(cudaMemcpyAsync(stage, h, R->seis.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (g.nrec > 0) {                     // staging is reused after the coef kernel (stream order)
+        RTM_CUDA(cudaMemcpyAsync(stage, R->seis.data(), R->seis.size() * sizeof(float), cudaMemcpyHostToDevice, s));
         RTM_CUDA(launch_transpose(stage, P->at<float>(P->L.seis_t), g.nrec, g.nt, s));
     }
     const size_t field = (size_t)g.dimx * g.pitch * sizeof(float);
@@ -207,14 +210,34 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
     RTM_CUDA(cudaMemsetAsync(P->base + P->L.img, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
     RTM_CUDA(cudaMemsetAsync(P->base + P->L.slf, 0, sizeof(double) * (size_t)g.nx * g.pitch, s));
     RTM_CUDA(cudaMemsetAsync(P->base + P->L.status, 0, 256, s));
+    std::vector<float>().swap(R->vel);
+    std::vector<float>().swap(R->seis);
     member_from_plan(P, S->mem[m]);
-    RTM_CUDA(cudaMemcpyAsync(S->d_mem + m, &S->mem[m], sizeof(BMember<float>), cudaMemcpyHostToDevice, s));
-    const int2 st = make_int2(1, 0);
-    RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &st, sizeof st, cudaMemcpyHostToDevice, s));
-    RTM_CUDA(cudaStreamSynchronize(s));         // host copies above come from stack/host data
+    S->pending.push_back(m);
     S->slot_plan[m] = P;
     S->slot_req[m] = R;
     R->t_admit = now_s();
+    return RTM_OK;
+}
+
+// Activates the members uploaded by admit: after the graph replay enqueued before them and
+// after their uploads, their descriptors and initial state (1, 0) are written and the work
+// lists rebuilt, all on the server's stream.
+static int activate(rtm_server *S)
+{
+    if (S->pending.empty()) return RTM_OK;
+    static const int2 kFirstStep = {1, 0};
+    RTM_CUDA(cudaEventRecord(S->up_ev, S->up));
+    RTM_CUDA(cudaStreamWaitEvent(S->stream, S->up_ev, 0));
+    for (int m : S->pending) {
+        RTM_CUDA(cudaMemcpyAsync(S->d_mem + m, &S->mem[m], sizeof(BMember<float>), cudaMemcpyHostToDevice,
+                                 S->stream));
+        RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &kFirstStep, sizeof kFirstStep, cudaMemcpyHostToDevice,
+                                 S->stream));
+    }
+    S->pending.clear();
+    rebuild_index(S);
+    RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
     return RTM_OK;
 }
 
@@ -229,16 +252,13 @@ static int harvest(rtm_server *S, int m)
     RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.slf), stage + n, 0, S->stream));
     R->img.resize(n);
     R->slf.resize(n);
-    float *h;
-    RTM_TRY(pinned(P, 2 * n * sizeof(float), &h));
-    RTM_CUDA(cudaMemcpyAsync(h, stage, 2 * n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+    RTM_CUDA(cudaMemcpyAsync(R->img.data(), stage, n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+    RTM_CUDA(cudaMemcpyAsync(R->slf.data(), stage + n, n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
     unsigned st = 0;
     RTM_CUDA(cudaMemcpyAsync(&st, P->base + P->L.status, sizeof st, cudaMemcpyDeviceToHost, S->stream));
     const int2 idle_state = make_int2(0, 0);
     RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &idle_state, sizeof idle_state, cudaMemcpyHostToDevice, S->stream));
     RTM_CUDA(cudaStreamSynchronize(S->stream));
-    memcpy(R->img.data(), h, n * sizeof(float));
-    memcpy(R->slf.data(), h + n, n * sizeof(float));
     R->t_done = now_s();
     S->cell_updates_done += 2LL * g.dimx * g.dimz * g.nt;
     S->done[R->id] = R;
@@ -327,6 +347,8 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
     }
     S->budget = hbm_budget_bytes;
     RTM_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    RTM_CUDA(cudaStreamCreateWithFlags(&S->up, cudaStreamNonBlocking));
+    RTM_CUDA(cudaEventCreateWithFlags(&S->up_ev, cudaEventDisableTiming));
     RTM_CUDA(cudaMalloc(&S->d_ix, sizeof(BatchIndex)));
     RTM_CUDA(cudaMalloc(&S->d_mem, sizeof(BMember<float>) * kMaxMembers));
     RTM_CUDA(cudaMalloc(&S->d_state, sizeof(int2) * kMaxMembers));
@@ -362,6 +384,7 @@ int rtm_server_destroy(rtm_server *S)
     }
     S->dcv.notify_all();
     for (auto &t : S->decoders) t.join();
+    cudaStreamSynchronize(S->up);
     cudaStreamSynchronize(S->stream);
     for (rtm_plan *P : S->slot_plan) if (P) plan_free(P);
     for (rtm_plan *P : S->idle) plan_free(P);
@@ -373,6 +396,8 @@ int rtm_server_destroy(rtm_server *S)
     cudaFreeHost(S->h_state);
     cudaEventDestroy(S->ev0); cudaEventDestroy(S->ev1);
     cudaEventDestroy(S->kev0); cudaEventDestroy(S->kev1);
+    cudaEventDestroy(S->up_ev);
+    cudaStreamDestroy(S->up);
     cudaStreamDestroy(S->stream);
     delete S;
     return RTM_OK;
@@ -426,14 +451,28 @@ int rtm_server_submit_zfp(rtm_server *S, const rtm_params *p, const float *veloc
     return RTM_OK;
 }
 
-// Admits what fits, runs steps_per_launch batched steps, harvests finished members.
+// Replays steps_per_launch batched steps of the active members, admits what fits while the
+// replay runs (uploads overlap it), activates the admitted members after it, and harvests
+// finished members.
 int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
 {
     if (!S) return fail(RTM_ERR_INVALID, "null server");
-    bool changed = false;
+    int active = 0;
+    for (int m = 0; m < S->max_members; ++m) active += S->slot_plan[m] != nullptr;
+    if (active > 0) {
+        RTM_CUDA(cudaEventRecord(S->ev0, S->stream));
+        RTM_CUDA(cudaGraphLaunch(S->gexec, S->stream));
+        RTM_CUDA(cudaEventRecord(S->ev1, S->stream));
+        S->launches += 3LL * S->steps_per_launch;
+    }
     // admission in arrival order among the requests whose inputs are ready (a request whose
-    // seismogram is still being decoded is passed over; one that does not fit blocks the rest)
+    // seismogram is still being decoded is passed over; one that does not fit blocks the
+    // rest), for as long as the replay runs: one request at least, then while the host time
+    // spent here stays below the previous replay's duration
+    const double t0 = now_s();
+    int admitted = 0;
     for (auto it = S->queue.begin(); it != S->queue.end();) {
+        if (admitted > 0 && (now_s() - t0) * 1e3 > S->last_replay_ms) break;
         ServeRequest *R = *it;
         const int ready = R->ready.load();
         if (ready == 0) { ++it; continue; }
@@ -455,25 +494,17 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
         const int st = admit(S, slot, R);
         if (st != RTM_OK) return st;
         it = S->queue.erase(it);
-        changed = true;
+        ++admitted;
     }
-    if (changed) {
-        rebuild_index(S);
-        RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
-    }
-    int active = 0;
-    for (int m = 0; m < S->max_members; ++m) active += S->slot_plan[m] != nullptr;
+    RTM_TRY(activate(S));
     if (active > 0) {
-        RTM_CUDA(cudaEventRecord(S->ev0, S->stream));
-        RTM_CUDA(cudaGraphLaunch(S->gexec, S->stream));
-        RTM_CUDA(cudaEventRecord(S->ev1, S->stream));
-        S->launches += 3LL * S->steps_per_launch;
         RTM_CUDA(cudaMemcpyAsync(S->h_state, S->d_state, sizeof(int2) * S->max_members,
                                  cudaMemcpyDeviceToHost, S->stream));
         RTM_CUDA(cudaStreamSynchronize(S->stream));
         float ms = 0.0f;
         RTM_CUDA(cudaEventElapsedTime(&ms, S->ev0, S->ev1));
         S->busy_ms += ms;
+        S->last_replay_ms = ms;
         if (S->kernel_sampled) {
             float kms = 0.0f;
             RTM_CUDA(cudaEventElapsedTime(&kms, S->kev0, S->kev1));
