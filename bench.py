@@ -59,6 +59,9 @@ def parse():
                     help="serving trace: Poisson-arriving requests (0: skip)")
     ap.add_argument("--serve-load", type=float, default=0.8,
                     help="arrival rate as a fraction of the batched service capacity")
+    ap.add_argument("--serve-load-high", type=float, default=1.5,
+                    help="second pass of the same trace at this load: a standing queue, the "
+                         "server full (0: skip)")
     ap.add_argument("--steps-per-launch", type=int, default=16,
                     help="batched steps per CUDA-graph replay of the server")
     ap.add_argument("--precision-nt", type=int, default=7500,
@@ -113,6 +116,11 @@ def workload(args, with_seis=True):
 
 def workload_name(p):
     return "rtm_single_shot_%dx%d_nt%d" % (p.nx, p.nz, p.nt)
+
+
+# the headline metric: Gcell-updates/s (value: the plain single-shot migration; the served
+# and batched forms, with p50/p99 latency and their ratio to the plain path, under their keys)
+METRIC = "RTM Gcell-updates/s + p50/p99 migration latency: served vs plain, rel-L2\u22641e-3"
 
 
 def algorithmic_bytes(p):
@@ -348,9 +356,9 @@ def run_batched(args, eng, rank=0, ws=1):
             "timing": "wall clock from the first submit (host buffers) to the last image on the host"}
 
 
-def run_served(args, eng, capacity_gcells):
-    """The serving trace: Poisson arrivals of migrations of mixed grids, nt and ring
-    precision at `serve_load` x the batched capacity; latency = finish - arrival."""
+def prepare_serving(args, eng):
+    """The serving trace's requests: mixed grids, nt and ring precision, each with its own
+    velocity realization and its seismogram as a ZFP tol 1e-4 stream."""
     from rtmuq2d_gb300 import synth, workloads
     reqs = workloads.serving_trace(args.serve_requests)
     templates = {}
@@ -374,8 +382,14 @@ def run_served(args, eng, capacity_gcells):
         g = synth.grf_coarse((p.nx, p.nz), p.dx, 200.0, r["seed"])
         ext = eng.extend_matrix(p, (mig.astype(np.float64) * np.exp(0.03 * g)).astype(np.float32))
         prepared.append((p, ext, wav, streams[key]))
+    return prepared, streams, tol
+
+
+def serve_trace(args, eng, prepared, tol, capacity_gcells, load):
+    """Poisson arrivals of the prepared requests at `load` x the batched capacity through one
+    server; latency = finish - arrival."""
     mean_cells = float(np.mean([p.cell_updates for p, *_ in prepared]))
-    rate = args.serve_load * capacity_gcells * 1e9 / mean_cells          # requests / s
+    rate = load * capacity_gcells * 1e9 / mean_cells          # requests / s
     rng = np.random.default_rng(29)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(prepared)))
     try:
@@ -383,7 +397,7 @@ def run_served(args, eng, capacity_gcells):
     except Exception:
         total_hbm = None
     srv = eng.Server(0, max_members=128, steps_per_launch=args.steps_per_launch)
-    done, occ, id_to_req = {}, [], {}
+    done, occ, resident, id_to_req = {}, [], [], {}
     t_start = time.monotonic()
     i = 0
     while len(done) < len(prepared):
@@ -394,6 +408,7 @@ def run_served(args, eng, capacity_gcells):
             i += 1
         active, queued = srv.step()
         occ.append(srv.stats()["bytes_in_use"])
+        resident.append(active)
         r = srv.poll()
         while r is not None:
             done[id_to_req[r[0]]] = r[3][2]
@@ -405,18 +420,31 @@ def run_served(args, eng, capacity_gcells):
     srv.close()
     lat = np.array([done[k] - (t_start + arrivals[k]) for k in range(len(prepared))])
     cells = sum(p.cell_updates for p, *_ in prepared)
-    return {"workload": "serving_trace_%d_requests" % len(prepared),
-            "requests": len(prepared), "value": cells / wall / 1e9, "unit": "Gcell-updates/s",
+    return {"value": cells / wall / 1e9, "unit": "Gcell-updates/s",
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "mean_latency_s": float(lat.mean()), "seconds": wall,
-            "arrival_rate_per_s": rate, "offered_load": args.serve_load,
+            "arrival_rate_per_s": rate, "offered_load": load,
             "gpu_busy_value": cells / (st["gpu_ms"] * 1e-3) / 1e9,
+            "resident_members_mean": float(np.mean(resident)), "resident_members_max": int(np.max(resident)),
             "hbm_occupancy_mean": (float(np.mean(occ)) / total_hbm) if total_hbm else None,
             "hbm_occupancy_max": (float(np.max(occ)) / total_hbm) if total_hbm else None,
-            "grids": [list(g) for g in workloads.SERVING_GRIDS], "nt_values": list(workloads.SERVING_NT),
-            "seismograms": "ZFP tol 1e-4 streams, decoded on the server's host threads",
-            "zfp_bytes_total": int(sum(len(x) for x in streams.values())),
-            "ring_precisions": ["fp32", "bf16"], "gpu_launches": st["launches"]}
+            "gpu_launches": st["launches"]}
+
+
+def run_served(args, eng, capacity_gcells):
+    """The serving trace at `serve_load` x the batched capacity (the latency view), and the
+    same trace at `serve_load_high` (a standing queue: the server's throughput when full)."""
+    from rtmuq2d_gb300 import workloads
+    prepared, streams, tol = prepare_serving(args, eng)
+    out = {"workload": "serving_trace_%d_requests" % len(prepared), "requests": len(prepared)}
+    out.update(serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load))
+    out.update({"grids": [list(g) for g in workloads.SERVING_GRIDS], "nt_values": list(workloads.SERVING_NT),
+                "seismograms": "ZFP tol 1e-4 streams, decoded on the server's host threads",
+                "zfp_bytes_total": int(sum(len(x) for x in streams.values())),
+                "ring_precisions": ["fp32", "bf16"]})
+    if args.serve_load_high > 0:
+        out["high_load"] = serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load_high)
+    return out
 
 
 def run_precision(args, eng):
@@ -499,7 +527,7 @@ def run_reference(args):
         vals.append(last["value"])
     v = float(np.mean(vals))
     cells_per_step = 2 * p.dim_x * p.dim_z * p.nt
-    line = {"impl": "reference", "metric": "RTM Gcell-updates/s (single-shot migration)", "value": v,
+    line = {"impl": "reference", "metric": METRIC, "value": v,
             "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cells_per_step / (v * 1e9) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -653,7 +681,7 @@ def run_gpu(args):
     if ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
         cpu.pop("seconds", None)
-    line = {"metric": "RTM Gcell-updates/s (single-shot migration)", "value": value,
+    line = {"metric": METRIC, "value": value,
             "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
