@@ -201,14 +201,6 @@ __device__ __forceinline__ T lap8(const T (&W)[9][4], const T (&zz)[12], int j)
         + (T)RTM_AC4 * (((W[0][j] + W[8][j]) + zz[0 + j]) + zz[8 + j]);
 }
 
-// First derivative along a strided line (B coefficients, :183-186 order).
-template <typename T>
-__device__ __forceinline__ T d1(const T *f, ptrdiff_t s)
-{
-    return (T)RTM_B4 * (f[4 * s] - f[-4 * s]) + (T)RTM_B3 * (f[3 * s] - f[-3 * s])
-         + (T)RTM_B2 * (f[2 * s] - f[-2 * s]) + (T)RTM_B1 * (f[s] - f[-s]);
-}
-
 template <int WARPS>
 __device__ __forceinline__ float block_max(float v, float *red)
 {

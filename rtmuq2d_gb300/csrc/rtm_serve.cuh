@@ -63,7 +63,6 @@ struct rtm_server {
     cudaEvent_t kev0 = nullptr, kev1 = nullptr;
     bool kernel_sampled = false;
     double kernel_ms_last = 0.0;
-    std::string err;
     // host threads decoding ZFP seismograms of submitted requests (rtm_server_submit_zfp)
     std::vector<std::thread> decoders;
     std::deque<rtm::ServeRequest *> to_decode;
@@ -116,12 +115,6 @@ static void member_from_plan(rtm_plan *P, BMember<float> &M)
     M.store_prec = P->p.precision;
     M.storage = P->p.storage;
     M.status = P->at<unsigned>(P->L.status);
-}
-
-static int server_fail(rtm_server *S, int code)
-{
-    S->err = rtm_last_error();
-    return code;
 }
 
 // Work lists of the current membership (inactive slots own no work).
