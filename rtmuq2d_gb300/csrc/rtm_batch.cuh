@@ -482,23 +482,28 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
             }
         }
     }
-    // The last CTA to finish advances every active member by one step: a forward pass has
-    // nt steps, a backward pass nt + 1 (the last one images only).
+    // The last CTA to finish advances every active member by one step (a forward pass has
+    // nt steps, a backward pass nt + 1, the last one images only), one member per thread.
+    __shared__ int s_last;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        const unsigned ticket = atomicAdd(done, 1u);
-        if (ticket == gridDim.x - 1) {
-            __threadfence();
-            for (int k = 0; k < nmem; ++k) {
-                int2 st = state[k];
-                if (st.x != 1 && st.x != 2) continue;
-                const int nt = ix->nt[k];
-                ++st.y;
-                if (st.x == 1 && st.y == nt) { st.x = 2; st.y = 0; }
-                else if (st.x == 2 && st.y > nt) { st.x = 3; st.y = 0; }
-                state[k] = st;
-            }
+        s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int k = threadIdx.x; k < nmem; k += blockDim.x) {
+            int2 st = s_state[k];                      // the state this step ran with
+            if (st.x != 1 && st.x != 2) continue;
+            const int nt = ix->nt[k];
+            ++st.y;
+            if (st.x == 1 && st.y == nt) { st.x = 2; st.y = 0; }
+            else if (st.x == 2 && st.y > nt) { st.x = 3; st.y = 0; }
+            state[k] = st;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
             done[2] = 0u;                              // k_mstep's chunk counter
             atomicExch(done, 0u);
             __threadfence();

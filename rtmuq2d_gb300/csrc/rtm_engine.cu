@@ -125,7 +125,9 @@ static int default_tile_x(const rtm_params &p)
     return it != g_tuned.end() ? it->second : 16;
 }
 
-static Geom make_geom(const rtm_params &p)
+// batched: a member of the batched step kernels, whose tiles carry no CPML work: z-tiles
+// are uniform (TZ rows from z = 0), so that no tile's TMA boxes load rows it does not use.
+static Geom make_geom(const rtm_params &p, bool batched = false)
 {
     Geom g;
     memset(&g, 0, sizeof g);
@@ -153,7 +155,9 @@ static Geom make_geom(const rtm_params &p)
     g.tiles_x = (g.dimx + g.tx - 1) / g.tx;
     // z-tile 0 holds the top CPML band (corrections, ring) and, when they sit just below
     // it, the receiver row and the shot, so that every other top tile is plain interior
-    {
+    if (batched) {
+        g.ztop = TZ;
+    } else {
         int top = g.thu - 4;
         if (g.zrec < g.thu + 16) top = std::max(top, g.zrec + 1);
         if (g.zs < g.thu + 16) top = std::max(top, g.zs + 1);
@@ -390,12 +394,12 @@ static int make_maps(rtm_plan *P)
     return make_plain_map(&P->tm_c, P->base + P->L.coef, P->g, P->es);
 }
 
-static int plan_alloc(const rtm_params &p, rtm_plan **out)
+static int plan_alloc(const rtm_params &p, rtm_plan **out, bool batched = false)
 {
     RTM_TRY(check_params(p));
     std::unique_ptr<rtm_plan> P(new rtm_plan());
     P->p = p;
-    P->g = make_geom(p);
+    P->g = make_geom(p, batched);
     P->L = make_layout(p, P->g);
     P->es = p.compute == RTM_COMPUTE_FP64 ? 8 : 4;
     cudaError_t e = cudaMalloc(&P->base, P->L.total);

@@ -171,7 +171,7 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
             plan_free(S->idle.back());
             S->idle.pop_back();
         }
-        RTM_TRY(plan_alloc(R->p, &P));
+        RTM_TRY(plan_alloc(R->p, &P, true));
         S->in_use += (long long)P->L.total;
         RTM_CUDA(cudaStreamSynchronize(P->stream));
         if (P->own_stream) cudaStreamDestroy(P->stream);
@@ -404,7 +404,7 @@ int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity,
     if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "the server runs FP32 migrations");
     rtm_params q = *p;
     q.tile_x = kBatchTileX;
-    const long long bytes = rtm_footprint_bytes(&q);
+    const long long bytes = (long long)make_layout(q, make_geom(q, true)).total;
     if (bytes > S->budget) return fail(RTM_ERR_NOMEM, "request needs %lld bytes, budget %lld", bytes, S->budget);
     auto *R = new ServeRequest();
     R->id = S->next_id++;
