@@ -69,12 +69,14 @@ def test_server_mixed_batch_equals_each_alone(engine):
     ids = [srv.submit(*c) for c in cases]
     out = srv.run_all()
     st = srv.stats()
+    kernel_ms = srv.kernel_ms()
     srv.close()
     for rid, (img, slf) in zip(ids, solo):
         assert np.array_equal(out[rid][0], img), rid
         assert np.array_equal(out[rid][1], slf), rid
     assert st["cell_updates"] == sum(c[0].cell_updates for c in cases)
     assert st["gpu_ms"] > 0 and st["launches"] > 0
+    assert 0.0 < kernel_ms < st["gpu_ms"]     # the tile kernel of one step, timed alone
 
 
 def test_server_admission_respects_budget(engine):
