@@ -519,7 +519,8 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
 {
     __shared__ int s_base[kMaxMembers + 1];
     __shared__ int2 s_state[kMaxMembers];
-    griddep_wait();
+    // This grid follows the step's k_mstep, which triggers it only after the previous step's
+    // k_bstrip has completed: the fields and state read here are final.  k_bstrip may launch.
     griddep_launch();
     const int nmem = ix->nmem;
     for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->psi_base[k];
@@ -542,6 +543,10 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
         const bool fresh = st.y == 0;
         psi_quad<T>(g, M.h1, u, M.psi, M.prof, strip, lq, fresh);
     }
+    // Every CTA waits for this step's k_mstep before it completes, so k_bstrip's wait on this
+    // grid also covers the tiles' u_next.
+    __syncthreads();
+    if (threadIdx.x == 0) griddep_wait();
 }
 
 // One batched step: every tile of every active member, in two phases (BatchIndex): phase 1
@@ -550,8 +555,9 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
 // strip (tile_coords order 0..nb-1).  Items go to CTAs in chunks of kChunk consecutive items,
 // so that consecutive items of a CTA mostly share their member and role; a CTA's first chunk
 // is its index, the later ones come from a step-wide counter (dynamic balance, single items
-// in the tail).  An NS-stage TMA pipeline is refilled by thread 0.  Tiles read no CPML data: k_bpsi of the same step
-// runs alongside, and k_bstrip completes the strip cells afterwards.
+// in the tail).  An NS-stage TMA pipeline is refilled by thread 0.  Tiles read no CPML data:
+// the step's k_bpsi follows (it fills the SMs this grid's tail frees), and k_bstrip completes
+// the strip cells afterwards.
 constexpr int kChunk = 4;
 constexpr int kTail = 2;                  // single-item grabs for the last kTail * G items
 
@@ -582,7 +588,6 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
         s_base2[k] = ix->base2[k];
     }
     for (int k = threadIdx.x; k < nmem; k += blockDim.x) {
-        s_state[k] = state[k];
         s_tiles[k] = (short)ix->tiles[k];
         s_nb[k] = (short)ix->nb[k];
         s_nt[k] = ix->nt[k];
@@ -592,6 +597,11 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
         fence_barrier_init();
     }
+    // the previous step (its k_bstrip wrote the strip cells and the state) has completed;
+    // only then may this step's k_bpsi launch
+    griddep_wait();
+    griddep_launch();
+    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
     __syncthreads();
     const int total1 = s_base1[nmem], total = total1 + s_base2[nmem];
     // Thread 0 maps the i-th work item of this CTA to (member, role, tile), builds the
@@ -695,7 +705,6 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) issue(s, s);
     }
-    griddep_launch();                    // k_bstrip of this step may launch; it waits for this grid
     for (int i = 0;; ++i) {
         const int s = i % NS;
         const uint32_t par = (uint32_t)((i / NS) & 1);
@@ -724,8 +733,4 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
         __syncthreads();
         if (threadIdx.x == 0) issue(i + NS, s);
     }
-    // Every CTA waits for this step's k_bpsi before it completes, so k_bstrip's wait on this
-    // grid also covers the psi it reads.
-    __syncthreads();
-    if (threadIdx.x == 0) griddep_wait();
 }

@@ -5,7 +5,7 @@
 // in arrival order while a member slot is free and their device footprint fits the HBM
 // budget; admission uploads the inputs and sets the member up (coef, seismogram transpose,
 // zeroed wavefields and image accumulators).  rtm_server_step replays a CUDA graph of
-// `steps_per_launch` batched time steps (k_bpsi + k_mstep + k_bstrip per step, chained by
+// `steps_per_launch` batched time steps (k_mstep + k_bpsi + k_bstrip per step, chained by
 // programmatic dependent launch): every active member advances one step per batched step,
 // whatever its grid, time axis or pass.  Members that finished their backward pass are harvested (image
 // and self image copied to host buffers) and their slots freed for the next admissions --
@@ -275,13 +275,13 @@ static int capture_graph(rtm_server *S)
     S->kernel_sampled = S->steps_per_launch >= 2;
     for (int k = 0; k < S->steps_per_launch && e == cudaSuccess; ++k) {
         const bool sample = S->kernel_sampled && k == 1;
-        e = launch_bpsi<float>(S->d_ix, S->d_mem, S->d_state, pgrid, k > 0, S->stream);
-        if (e == cudaSuccess && sample) e = cudaEventRecordWithFlags(S->kev0, S->stream, cudaEventRecordExternal);
+        if (sample) e = cudaEventRecordWithFlags(S->kev0, S->stream, cudaEventRecordExternal);
         if (e == cudaSuccess)
-            e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, !sample, S->stream);
+            e = launch_bstep<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, grid, k > 0 && !sample, S->stream);
         if (e == cudaSuccess && sample) e = cudaEventRecordWithFlags(S->kev1, S->stream, cudaEventRecordExternal);
+        if (e == cudaSuccess) e = launch_bpsi<float>(S->d_ix, S->d_mem, S->d_state, pgrid, !sample, S->stream);
         if (e == cudaSuccess)
-            e = launch_bstrip<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, pgrid, !sample, S->stream);
+            e = launch_bstrip<float>(S->d_ix, S->d_mem, S->d_state, S->d_done, pgrid, 1, S->stream);
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(S->stream, &graph);
