@@ -35,6 +35,10 @@ int adjointModeling(int simId, int *shot, float *velocity, float *wavelet, float
                     float *imageCondition, float *selfImageCondition);
 int zfp2d_lossyDecompression(char *zfp_data_02, float *array, int dimension1, int dimension2,
                              float tolerance);                                   /* compression_tools.h:9 */
+/* compression_tools.h:5: *compression = a malloc'ed buffer holding the stream (the caller
+ * frees it), the stream's byte length returned (0 on failure, as zfp_compress). */
+int zfp2d_lossyCompression(void **compression, float *array, int dimension1, int dimension2,
+                           float tolerance);
 void cross_correlation(float *imageCondition, float *sourceWavefield, float *receiverWavefield);
 void normalized_cross_correlation(float *imageCondition, float *selfImageCondition,
                                   float *sourceWavefield, float *receiverWavefield);

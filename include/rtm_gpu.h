@@ -310,6 +310,14 @@ typedef struct rtm_survey {
  * float32 as the reference stacks them; both output files are written.  RTM_ERR_IO when an
  * input cannot be read or an output written (the reference exits instead). */
 int rtm_routine_run(const rtm_params *p, const rtm_survey *survey, int simulation_id);
+/* rtm_routine over several simulations on one GPU (replaces the MPI fan-out of
+ * mpi_rtm_iso2d.c:39-51): every (simulation, shot) migration is a request of one batched
+ * server (rtm_server_*; budget and member slots as rtm_server_create takes them, 0 = default),
+ * so the simulations' shots run resident together; per simulation the same files and outputs
+ * as rtm_routine_run, the images summed in shot order.  Each shot's seismogram file is read
+ * once and decoded per request on the server's host threads. */
+int rtm_routine_batch(const rtm_params *p, const rtm_survey *survey, const int *simulation_ids,
+                      int n_simulations, long long hbm_budget_bytes, int max_members);
 
 #ifdef __cplusplus
 }

@@ -175,6 +175,7 @@ def _declare(L):
         "rtm_zfp_encode_float2d": (C.c_int, [fp, C.c_int, C.c_int, C.c_double, vp, C.c_size_t,
                                              C.POINTER(C.c_size_t)]),
         "rtm_routine_run": (C.c_int, [P, C.POINTER(RtmSurvey), C.c_int]),
+        "rtm_routine_batch": (C.c_int, [P, C.POINTER(RtmSurvey), ip, C.c_int, C.c_longlong, C.c_int]),
         "rtm_plan_profile": (C.c_int, [vp, C.c_int]),
         "rtm_plan_profile_read": (C.c_int, [vp, C.POINTER(C.c_double), ip, C.POINTER(C.c_double), ip]),
     }
@@ -199,7 +200,7 @@ def exported_symbols():
             "rtm_server_step",
             "rtm_server_poll", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
             "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
-            "rtm_zfp_encode_float2d", "rtm_routine_run"]
+            "rtm_zfp_encode_float2d", "rtm_routine_run", "rtm_routine_batch"]
 
 
 def status_string(st: int) -> str:
@@ -345,6 +346,15 @@ def zfp_encode(field: np.ndarray, tolerance: float) -> bytes:
 def routine_run(p: RtmParams, survey: RtmSurvey, simulation_id: int) -> None:
     """The migration driver of one simulation on files (rtm_iso2d.c:15-177)."""
     _check(lib().rtm_routine_run(C.byref(p), C.byref(survey), simulation_id))
+
+
+def routine_batch(p: RtmParams, survey: RtmSurvey, simulation_ids, hbm_budget_bytes: int = 0,
+                  max_members: int = 0) -> None:
+    """rtm_routine over several simulations through one batched server (the reference's MPI
+    fan-out, on one GPU): per simulation the same output files as routine_run."""
+    ids = (C.c_int * len(simulation_ids))(*[int(i) for i in simulation_ids])
+    _check(lib().rtm_routine_batch(C.byref(p), C.byref(survey), ids, len(simulation_ids),
+                                   int(hbm_budget_bytes), int(max_members)))
 
 
 def dropin_lib():

@@ -108,3 +108,137 @@ done:
     free(img); free(slf); free(stack); free(lap);
     return st;
 }
+
+/* Whole file as bytes (a ZFP stream). */
+static int read_bytes(const char *path, unsigned char **out, size_t *n)
+{
+    *out = NULL;
+    *n = 0;
+    FILE *f = fopen(path, "rb");
+    if (!f) return RTM_ERR_IO;
+    int st = RTM_ERR_IO;
+    if (fseek(f, 0, SEEK_END) == 0) {
+        const long len = ftell(f);
+        if (len >= 0 && fseek(f, 0, SEEK_SET) == 0) {
+            unsigned char *b = (unsigned char *)malloc(len > 0 ? (size_t)len : 1);
+            if (!b) st = RTM_ERR_NOMEM;
+            else if (fread(b, 1, (size_t)len, f) == (size_t)len) {
+                *out = b;
+                *n = (size_t)len;
+                st = RTM_OK;
+            } else {
+                free(b);
+            }
+        }
+    }
+    fclose(f);
+    return st;
+}
+
+/*
+ * Several simulations' migrations through one batched server: the reference fans
+ * rtm_routine(simulation) out over MPI ranks (mpi_rtm_iso2d.c:39-51); here every (simulation,
+ * shot) migration is a request of one rtm_server on this GPU, so the UQ realizations and
+ * their shots run resident together.  Per simulation the same files and outputs as
+ * rtm_routine_run: the shots' images summed in float32 in shot order (an image that finishes
+ * early waits for its predecessors), the stack and its Laplacian written.  Each shot's ZFP
+ * stream (keyed by shot id, as the reference keys it) is read once and decoded per request
+ * by the server's host threads while the GPU steps.
+ */
+int rtm_routine_batch(const rtm_params *params, const rtm_survey *s, const int *simulation_ids,
+                      int n_simulations, long long hbm_budget_bytes, int max_members)
+{
+    if (!params || !s || !simulation_ids || n_simulations < 1 || !s->velocity_file || !s->wavelet_file ||
+        !s->seismogram_file || !s->stacked_file || !s->laplacian_file || s->n_shots < 0)
+        return RTM_ERR_INVALID;
+    rtm_params p = *params;
+    p.shot_x = s->first_shot;
+    p.shot_z = s->shot_depth;
+    int st = rtm_params_check(&p);
+    if (st != RTM_OK) return st;
+    if (max_members < 1 || max_members > 128) max_members = 128;
+    const int n_shots = s->n_shots;
+    const size_t nimg = (size_t)p.nx * (size_t)p.nz;
+    const size_t next = (size_t)(p.th_left + p.nx + p.th_right) * (size_t)(p.th_up + p.nz + p.th_down);
+    const size_t nwav = p.n_wavelet > 0 ? (size_t)p.n_wavelet : 1;
+    const size_t n_req = (size_t)n_simulations * (size_t)n_shots;
+    float *model = (float *)calloc(nimg, sizeof(float));
+    float *ext = (float *)calloc(next, sizeof(float));
+    float *wav = (float *)calloc(nwav, sizeof(float));
+    float *img = (float *)calloc(nimg, sizeof(float));
+    float *slf = (float *)calloc(nimg, sizeof(float));
+    float *lap = (float *)calloc(nimg, sizeof(float));
+    float *stack = (float *)calloc(nimg * (size_t)n_simulations, sizeof(float));
+    unsigned char **zs = (unsigned char **)calloc(n_shots > 0 ? (size_t)n_shots : 1, sizeof(*zs));
+    size_t *zb = (size_t *)calloc(n_shots > 0 ? (size_t)n_shots : 1, sizeof(*zb));
+    long long *ids = (long long *)calloc(n_req > 0 ? n_req : 1, sizeof(*ids));
+    float **held = (float **)calloc(n_req > 0 ? n_req : 1, sizeof(*held));   /* finished, not yet summed */
+    int *next_shot = (int *)calloc((size_t)n_simulations, sizeof(int));
+    rtm_server *srv = NULL;
+    char path[RTM_PATH_LEN];
+    if (!model || !ext || !wav || !img || !slf || !lap || !stack || !zs || !zb || !ids || !held || !next_shot) {
+        st = RTM_ERR_NOMEM;
+        goto done;
+    }
+    if (p.n_wavelet > 0 && (st = read_raw(s->wavelet_file, wav, (size_t)p.n_wavelet)) != RTM_OK) goto done;
+    for (int k = 0; k < n_shots; ++k) {
+        if ((st = format_path(path, s->seismogram_file, k + 1)) != RTM_OK) goto done;
+        if ((st = read_bytes(path, &zs[k], &zb[k])) != RTM_OK) goto done;
+    }
+    if ((st = rtm_server_create(hbm_budget_bytes, max_members, 16, &srv)) != RTM_OK) goto done;
+    for (int i = 0; i < n_simulations; ++i) {
+        if ((st = format_path(path, s->velocity_file, simulation_ids[i])) != RTM_OK) goto done;
+        if ((st = read_raw(path, model, nimg)) != RTM_OK) goto done;
+        rtm_extend_matrix(&p, ext, model);
+        for (int k = 0; k < n_shots; ++k) {
+            p.shot_x = s->first_shot + k * s->shot_spacing;
+            p.shot_z = s->shot_depth;
+            st = rtm_server_submit_zfp(srv, &p, ext, wav, zs[k], zb[k], s->zfp_tolerance,
+                                       &ids[(size_t)i * n_shots + k]);
+            if (st != RTM_OK) goto done;
+        }
+    }
+    for (size_t finished = 0; finished < n_req;) {
+        int active = 0, queued = 0;
+        if ((st = rtm_server_step(srv, &active, &queued)) != RTM_OK) goto done;
+        for (;;) {
+            long long rid = 0;
+            st = rtm_server_poll(srv, &rid, img, slf, NULL);
+            if (st == RTM_ERR_BUSY) { st = RTM_OK; break; }
+            if (st != RTM_OK) goto done;
+            size_t r = 0;
+            while (r < n_req && ids[r] != rid) ++r;
+            if (r == n_req) { st = RTM_ERR_INVALID; goto done; }
+            held[r] = (float *)malloc(nimg * sizeof(float));
+            if (!held[r]) { st = RTM_ERR_NOMEM; goto done; }
+            memcpy(held[r], img, nimg * sizeof(float));
+            ++finished;
+            /* rtm_iso2d.c:121-126: float sum in shot order */
+            const int i = (int)(r / (size_t)n_shots);
+            float *stk = stack + (size_t)i * nimg;
+            while (next_shot[i] < n_shots && held[(size_t)i * n_shots + next_shot[i]]) {
+                float *im = held[(size_t)i * n_shots + next_shot[i]];
+                for (size_t q = 0; q < nimg; ++q) stk[q] = stk[q] + im[q];
+                free(im);
+                held[(size_t)i * n_shots + next_shot[i]] = NULL;
+                ++next_shot[i];
+            }
+        }
+        if (finished < n_req && active == 0 && queued == 0) { st = RTM_ERR_INVALID; goto done; }
+    }
+    for (int i = 0; i < n_simulations; ++i) {
+        const float *stk = stack + (size_t)i * nimg;
+        if ((st = format_path(path, s->stacked_file, simulation_ids[i])) != RTM_OK) goto done;
+        if ((st = write_raw(path, stk, nimg)) != RTM_OK) goto done;
+        if ((st = rtm_laplacian_filter2D(&p, lap, stk)) != RTM_OK) goto done;
+        if ((st = format_path(path, s->laplacian_file, simulation_ids[i])) != RTM_OK) goto done;
+        if ((st = write_raw(path, lap, nimg)) != RTM_OK) goto done;
+    }
+done:
+    if (srv) rtm_server_destroy(srv);
+    if (held) for (size_t r = 0; r < n_req; ++r) free(held[r]);
+    if (zs) for (int k = 0; k < n_shots; ++k) free(zs[k]);
+    free(model); free(ext); free(wav); free(img); free(slf); free(lap); free(stack);
+    free(zs); free(zb); free(ids); free(held); free(next_shot);
+    return st;
+}

@@ -98,6 +98,23 @@ int zfp2d_lossyDecompression(char *zfp_data_02, float *array, int dimension1, in
     return 0;
 }
 
+/* compression_tools.c:10-71: the stream zfp_compress writes for the field (dimension1 fastest)
+ * at this accuracy, in a malloc'ed buffer of the library's maximum size */
+int zfp2d_lossyCompression(void **compression, float *array, int dimension1, int dimension2, float tolerance)
+{
+    *compression = NULL;
+    const size_t cap = rtm_zfp_encode_bound(dimension1, dimension2);
+    void *buf = malloc(cap > 0 ? cap : 1);
+    if (!buf) return 0;
+    size_t used = 0;
+    if (rtm_zfp_encode_float2d(array, dimension1, dimension2, tolerance, buf, cap, &used) != RTM_OK) {
+        free(buf);
+        return 0;
+    }
+    *compression = buf;
+    return (int)used;
+}
+
 /* image_conditions.c:8: the image only (the self image goes to a scratch buffer) */
 void cross_correlation(float *imageCondition, float *sourceWavefield, float *receiverWavefield)
 {

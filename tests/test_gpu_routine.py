@@ -66,3 +66,24 @@ def test_routine_missing_input_is_an_io_error(engine, tmp_path):
     with pytest.raises(engine.RtmError) as e:
         engine.routine_run(p, s, sim_id)
     assert e.value.status == 6
+
+
+def test_routine_batch_matches_routine_per_simulation(engine, tmp_path):
+    """Two simulations (two velocity files) with their shots through one batched server: each
+    simulation's stack equals the single-simulation driver's (<= 1e-5: the batched kernels,
+    same scheme), its Laplacian -- a second derivative, which amplifies the stack's last-bit
+    differences -- within the image bar 1e-4, and both the reference's (<= 1e-4)."""
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    other = sim_id + 7
+    model = d["uneven/model"].astype(np.float32)
+    (model * np.float32(1.03)).tofile(tmp_path / "INPUTS" / ("vp_%05d.bin" % other))
+    engine.routine_batch(p, s, [sim_id, other], max_members=3)
+    batch = {k: _outputs(d, tmp_path, k) for k in (sim_id, other)}
+    for k in (sim_id, other):
+        engine.routine_run(p, s, k)
+        single = _outputs(d, tmp_path, k)
+        assert rel_l2(batch[k][0], single[0]) <= 1e-5, k
+        assert rel_l2(batch[k][1], single[1]) <= 1e-4, k
+    assert rel_l2(batch[sim_id][0], d["routine/stacked"]) <= 1e-4
+    assert rel_l2(batch[sim_id][1], d["routine/laplacian"]) <= 1e-4
+    assert rel_l2(batch[other][0], batch[sim_id][0]) > 1e-3     # the second model differs

@@ -98,3 +98,23 @@ def test_encode_decode_round_trip_bound(engine):
         assert np.abs(out - f).max() <= tol
     lossless = engine.zfp_decode(engine.zfp_encode(f, 0.0), 33, 45, 0.0)
     assert np.abs(lossless - f).max() <= 1e-6 * np.abs(f).max()
+
+
+@pytest.mark.parametrize("tag,tol", (("tol1e-4", 1e-4), ("tol0", 0.0)))
+def test_dropin_compression_matches_reference_stream(engine, tag, tol):
+    """zfp2d_lossyCompression (compression_tools.h:5) through the drop-in library: a malloc'ed
+    buffer holding the reference's stream byte for byte, its length returned."""
+    import ctypes as C
+    d = load()
+    inp = np.ascontiguousarray(d["zfp/input"], np.float32)
+    L = engine.dropin_lib()
+    L.zfp2d_lossyCompression.restype = C.c_int
+    L.zfp2d_lossyCompression.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                         C.c_float]
+    buf = C.c_void_p()
+    n = L.zfp2d_lossyCompression(C.byref(buf), inp.ctypes.data_as(C.POINTER(C.c_float)), inp.shape[0],
+                                 inp.shape[1], C.c_float(tol))
+    ref = d["zfp/%s/stream" % tag].tobytes()
+    assert n == len(ref) and buf.value
+    assert C.string_at(buf.value, n) == ref
+    C.CDLL(None).free(buf)
