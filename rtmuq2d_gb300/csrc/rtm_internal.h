@@ -86,6 +86,14 @@ __host__ __device__ __forceinline__ void tile_coords(const Geom &g, int t, int &
     zt = 1 + t % nzi;
 }
 
+// Tiles of the top and bottom z-tile rows and of the left/right CPML x-tiles of the other
+// rows: the first boundary_tiles(g) tiles of tile_coords' order.
+__host__ __device__ __forceinline__ int boundary_tiles(const Geom &g)
+{
+    const int nzb = g.tiles_z > 1 ? 2 : 1;
+    return g.tiles_x * nzb + (g.nxl + (g.tiles_x - g.xr0)) * (g.tiles_z - nzb);
+}
+
 __host__ __device__ __forceinline__ int ztile_origin(const Geom &g, int zt)
 {
     return zt == 0 ? 0 : g.ztop + (zt - 1) * TZ;

@@ -639,11 +639,7 @@ int strip_blocks_host(const Geom &g)
     return round_block(c.nA + c.nB) / kStripBlock;
 }
 
-int boundary_tiles_host(const Geom &g)
-{
-    const int nzb = g.tiles_z > 1 ? 2 : 1;
-    return g.tiles_x * nzb + (g.nxl + (g.tiles_x - g.xr0)) * (g.tiles_z - nzb);
-}
+int boundary_tiles_host(const Geom &g) { return boundary_tiles(g); }
 
 template <typename T>
 static cudaError_t configure_bstep()
