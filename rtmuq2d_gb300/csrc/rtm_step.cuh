@@ -528,12 +528,15 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
     }
     __syncthreads();
     // Static balanced schedule over the boundary-first order (tile_coords): CTA b takes the
-    // boundary tiles b, b + G, ... (the slow ones: CPML, ring, source, receivers), then a
-    // contiguous range of interior tiles.  The r = nb mod G CTAs that carry one boundary tile
-    // more take kBalance interior tiles fewer, a boundary tile counting as 1 + kBalance
-    // interior ones (measured on 3400 x 700: forward 24.5 -> 22.5 us, backward 38.2 -> 36.7 us
-    // per step against plain round-robin); the ranges partition the interior exactly.  A
-    // stage with no tile left still completes its barrier phase.
+    // boundary tiles b, b + G, ... (the slow ones: CPML, ring, source, receivers), then its
+    // share of the interior tiles.  The r = nb mod G CTAs that carry one boundary tile more
+    // take kBalance interior tiles fewer, a boundary tile counting as 1 + kBalance interior
+    // ones.  The interior goes out in rounds -- round j gives one tile to every CTA with more
+    // than j interior tiles, in CTA order -- so that all CTAs sweep the grid together (their
+    // halos and, backward, the image and source rows stay in L2).  Measured on 3400 x 700
+    // against plain round-robin: forward 24.5 -> 22.6 us, backward 38.2 -> 30.9 us per step.
+    // Every tile is taken exactly once.  A stage with no tile left still completes its
+    // barrier phase.
     constexpr int kBalance = BWD ? 2 : 3;
     const int G = gridDim.x, b = blockIdx.x;
     const int nb = boundary_tiles(g), ni = g.tiles - nb;
@@ -542,17 +545,22 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
     int xlo = (ni + r * kBalance) / G, xhi = xlo - kBalance;  // interior tiles for b >= r, b < r
     if (xhi < 0) { xhi = 0; xlo = ni / (G - r); }
     const int rem = ni - r * xhi - (G - r) * xlo;            // one more each: b >= r first
-    const int ex = max(0, rem - (G - r));
-    int cnt, start;
-    if (b < r) {
-        cnt = xhi + ((G - r + b) < rem ? 1 : 0);
-        start = b * xhi + min(b, ex);
-    } else {
-        cnt = xlo + ((b - r) < rem ? 1 : 0);
-        start = r * xhi + min(r, ex) + (b - r) * xlo + min(b - r, rem);
-    }
+    const int ex = max(0, rem - (G - r)), nc = min(rem, G - r);
+    // CTA groups by interior count: [0,ex) xhi+1, [ex,r) xhi, [r,r+nc) xlo+1, [r+nc,G) xlo
+    const int cnt = b < r ? xhi + (b < ex ? 1 : 0) : xlo + (b - r < nc ? 1 : 0);
+    auto interior = [&](int j) {          // position of this CTA's j-th interior tile
+        const int lo[4] = {0, ex, r, r + nc}, hi[4] = {ex, r, r + nc, G};
+        const int c[4] = {xhi + 1, xhi, xlo + 1, xlo};
+        int p = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            p += min(j, c[k]) * (hi[k] - lo[k]);               // rounds before j
+            if (c[k] > j) p += max(0, min(b, hi[k]) - lo[k]);  // CTAs before b in round j
+        }
+        return p;
+    };
     auto issue = [&](int i, int s) {
-        const int t = i < kb ? b + i * G : (i - kb < cnt ? nb + start + (i - kb) : g.tiles);
+        const int t = i < kb ? b + i * G : (i - kb < cnt ? nb + interior(i - kb) : g.tiles);
         tile_of[s] = t;
         if (t >= g.tiles) {
             mbar_arrive(&full[s]);
