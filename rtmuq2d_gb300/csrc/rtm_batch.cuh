@@ -438,8 +438,9 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
             if (save) {
                 void *slot = member_slot(M, st.y + 1);
                 int ri[4];
+                const bool rq = have && ring_quad(g, x, zq);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) ri[j] = (have && zq + j < g.dimz) ? ring_index(g, x, zq + j) : -1;
+                for (int j = 0; j < 4; ++j) ri[j] = (rq && zq + j < g.dimz) ? ring_index(g, x, zq + j) : -1;
                 if (M.store_prec == 0) {
 #pragma unroll
                     for (int j = 0; j < 4; ++j)

@@ -614,12 +614,16 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
     PsiArgs<T> q;
     fill_psi<T>(P, a, q);
     const bool ring = P->p.storage == RTM_STORE_RING;
+    // FP32 rings are saved by the psi kernel of the next step (slot t holds u_t), the last one
+    // by a ring-only pass after the loop; 16-bit rings by the step kernel (per-tile scales)
+    const bool ring_psi = ring && P->p.precision == RTM_PREC_FP32;
     (void)step_grid<T>(0, g);            // configure the kernels before any capture
     auto loop = [&]() -> int {
         int c = 0;
         StepMaps maps;
         for (int t = 0; t < g.nt; ++t) {
             q.u = u[c];
+            q.ring = ring_psi && t >= 1 ? static_cast<T *>(slot_ptr(P, t)) : nullptr;
             RTM_CUDA(launch_psi<T>(q, t > 0 && !sampled(P, t - 1), s));
             a.u_next = u[1 - c];
             a.t = t;
@@ -628,11 +632,11 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
             if (d_seis_out && g.nrec > 0) f |= F_RECORD;
             a.store = nullptr;
             a.store_scale = nullptr;
-            if (ring) {
+            if (ring && !ring_psi) {
                 f |= F_RING_SAVE;
                 a.store = slot_ptr(P, t + 1);
                 a.store_scale = scale_ptr(P, t + 1);
-            } else if (t % g.slices == 0) {
+            } else if (!ring && t % g.slices == 0) {
                 f |= F_SNAP_SAVE;
                 a.store = slot_ptr(P, t / g.slices);
                 a.store_scale = scale_ptr(P, t / g.slices);
@@ -646,6 +650,14 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
             RTM_TRY(timed_step<T>(P, 0, t, maps, a));
             P->launches += 2;
             c ^= 1;
+        }
+        if (ring_psi) {                  // the ring of u_nt
+            PsiArgs<T> r = q;
+            r.u = u[c];
+            r.ring = static_cast<T *>(slot_ptr(P, g.nt));
+            r.ring_only = 1;
+            RTM_CUDA(launch_psi<T>(r, !sampled(P, g.nt - 1), s));
+            P->launches++;
         }
         return RTM_OK;
     };

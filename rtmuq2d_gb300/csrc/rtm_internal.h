@@ -194,6 +194,8 @@ struct PsiArgs {
     const T *u;                 // current wavefield
     T *psi_l, *psi_r, *psi_t, *psi_b;
     const float *a_l, *b_l, *a_r, *b_r, *a_t, *b_t, *a_b, *b_b;
+    T *ring;                    // forward, FP32 ring storage: u's ring cells go to this slot
+    int ring_only;              // save the ring only (after the last forward step)
 };
 
 // ---- batched steps (rtm_batch.cuh) -------------------------------------------------------

@@ -157,6 +157,15 @@ __device__ __forceinline__ int ring_index(const Geom &g, int x, int z)
     return -1;
 }
 
+// Whether the quad [zq, zq+4) of column x holds a ring cell (a cheap test before ring_index):
+// the top and bottom bands span the ring box's columns, the side bands its rows.
+__device__ __forceinline__ bool ring_quad(const Geom &g, int x, int zq)
+{
+    if (x < g.rx0 - 4 || x >= g.rx1 + 4) return false;
+    if (x < g.rx0 || x >= g.rx1) return zq < g.rz1 + 4 && zq + 4 > g.rz0 - 4;
+    return (zq < g.rz0 && zq + 4 > g.rz0 - 4) || (zq < g.rz1 + 4 && zq + 4 > g.rz1);
+}
+
 __device__ __forceinline__ bool in_region(const Geom &g, int x, int z)
 {
     return x >= g.rx0 && x < g.rx1 && z >= g.rz0 && z < g.rz1;
@@ -301,17 +310,62 @@ __device__ __forceinline__ void psi_quad(const Geom &g, T h1, const T *u0, T *co
     st4(ps4, ps);
 }
 
+// Ring cells of psi quad (strip, idx) of k_psi's enumeration (psi_quad's decode), copied from
+// u to the ring slot: the side bands (corners included) by the left/right quads, the top and
+// bottom bands between them by the top/bottom quads -- every ring cell once.
+template <typename T>
+__device__ __forceinline__ void ring_save_quad(const Geom &g, const T *u, T *ring, int strip, int idx)
+{
+    int x, zq;
+    if (strip == 0 || strip == 2) {
+        const int th = strip == 0 ? g.thl : g.thr;
+        const int nq = (g.dimz - 8 + 3) / 4;
+        if (idx >= (th - 8) * nq) return;
+        const int li = 4 + idx / nq;
+        zq = 4 + 4 * (idx % nq);
+        x = strip == 0 ? li : g.dimx - g.thr + li;
+        if (x >= g.rx0 && x < g.rx1) return;
+    } else {
+        int nq, z0;
+        if (strip == 1) {
+            nq = (g.thu - 8 + 3) / 4;
+            z0 = 4;
+        } else {
+            z0 = (g.dimz - g.thd + 4) & ~3;
+            nq = (g.dimz - 4 - z0 + 3) / 4;
+        }
+        if (idx >= (g.dimx - 8) * nq) return;
+        x = 4 + idx / nq;
+        zq = z0 + 4 * (idx % nq);
+        if (x < g.rx0 || x >= g.rx1) return;
+    }
+    if (!ring_quad(g, x, zq)) return;
+    const T *col = u + (size_t)x * g.pitch;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = zq + j;
+        const int r = z < g.dimz ? ring_index(g, x, z) : -1;
+        if (r >= 0) ring[r] = col[z];
+    }
+}
+
 // Plain-plan psi kernel (blockIdx.y = strip).  With programmatic dependent launch it first
 // waits for the previous step kernel (whose output u_n it reads), then lets the next step
-// kernel start.
+// kernel start.  Forward with FP32 ring storage it also saves u_n's ring (slot n): done here,
+// on the strip quads, instead of inside the step kernel's boundary tiles (forward step 22.5 ->
+// 20.3 us on 3400 x 700).
 template <typename T>
 __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> a)
 {
     griddep_wait();
     griddep_launch();
-    T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
-    const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
-    psi_quad<T>(a.g, a.h1, a.u, psi, prof, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, false);
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!a.ring_only) {
+        T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
+        const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
+        psi_quad<T>(a.g, a.h1, a.u, psi, prof, blockIdx.y, idx, false);
+    }
+    if (a.ring) ring_save_quad<T>(a.g, a.u, a.ring, blockIdx.y, idx);
 }
 
 #include "rtm_march.cuh"

@@ -379,13 +379,14 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
                 }
             }
             st4(a.u_next + (size_t)x * P + zq, v[r]);
-            if (!BWD && (ring_t || snap_t)) {
+            const bool ring_q = ring_t && ring_quad(g, x, zq);
+            if (!BWD && (ring_q || snap_t)) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int z = zq + j;
                     if (z >= g.dimz) continue;
                     size_t o = (size_t)-1;
-                    if (ring_t) {
+                    if (ring_q) {
                         const int idx = ring_index(g, x, z);
                         if (idx >= 0) o = (size_t)idx;
                     }
@@ -412,7 +413,7 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
                 for (int j = 0; j < 4; ++j) {
                     const int x = xb + r, z = zq + j;
                     if (!zok || x >= g.dimx || z >= g.dimz) continue;
-                    if (ring_t) {
+                    if (ring_t && ring_quad(g, x, zq)) {
                         const int idx = ring_index(g, x, z);
                         if (idx >= 0) store_put<T>(a.store, a.store_prec, (size_t)idx, v[r][j], inv);
                     }
@@ -458,7 +459,7 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
                 for (int j = 0; j < 4; ++j)
                     if (zq + j == g.zs) s[j] = add_source<T>(a.wavelet, tsrc, s[j], cf[j]);
             }
-            if (col_ok && ring_t) {
+            if (col_ok && ring_t && ring_quad(g, x, zq)) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int z = zq + j;
