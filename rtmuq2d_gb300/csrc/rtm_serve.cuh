@@ -37,6 +37,7 @@ struct rtm_server {
     cudaStream_t up = nullptr;
     cudaEvent_t up_ev = nullptr;
     std::vector<int> pending;              // slots uploaded, not yet activated
+    std::vector<int> finished;             // slots whose member finished, not yet harvested
     double last_replay_ms = 0.0;
     // device side
     rtm::BatchIndex *d_ix = nullptr;
@@ -234,6 +235,9 @@ static int activate(rtm_server *S)
     return RTM_OK;
 }
 
+// A finished member's image and self image to its request, on the upload stream: the graph
+// replaying meanwhile skips the member (its state is past its backward pass), so the copies
+// overlap the replay.  The slot is free afterwards.
 static int harvest(rtm_server *S, int m)
 {
     rtm_plan *P = S->slot_plan[m];
@@ -241,17 +245,18 @@ static int harvest(rtm_server *S, int m)
     const Geom &g = P->g;
     const size_t n = (size_t)g.nx * g.nz;
     float *stage = P->at<float>(P->L.staging);
-    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.img), stage, 0, S->stream));
-    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.slf), stage + n, 0, S->stream));
+    cudaStream_t s = S->up;
+    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.img), stage, 0, s));
+    RTM_CUDA(launch_image_out<float>(g, P->at<double>(P->L.slf), stage + n, 0, s));
     R->img.resize(n);
     R->slf.resize(n);
-    RTM_CUDA(cudaMemcpyAsync(R->img.data(), stage, n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
-    RTM_CUDA(cudaMemcpyAsync(R->slf.data(), stage + n, n * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+    RTM_CUDA(cudaMemcpyAsync(R->img.data(), stage, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    RTM_CUDA(cudaMemcpyAsync(R->slf.data(), stage + n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     unsigned st = 0;
-    RTM_CUDA(cudaMemcpyAsync(&st, P->base + P->L.status, sizeof st, cudaMemcpyDeviceToHost, S->stream));
-    const int2 idle_state = make_int2(0, 0);
-    RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &idle_state, sizeof idle_state, cudaMemcpyHostToDevice, S->stream));
-    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    RTM_CUDA(cudaMemcpyAsync(&st, P->base + P->L.status, sizeof st, cudaMemcpyDeviceToHost, s));
+    static const int2 kIdle = {0, 0};
+    RTM_CUDA(cudaMemcpyAsync(S->d_state + m, &kIdle, sizeof kIdle, cudaMemcpyHostToDevice, s));
+    RTM_CUDA(cudaStreamSynchronize(s));
     R->t_done = now_s();
     S->cell_updates_done += 2LL * g.dimx * g.dimz * g.nt;
     S->done[R->id] = R;
@@ -452,12 +457,17 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
     if (!S) return fail(RTM_ERR_INVALID, "null server");
     int active = 0;
     for (int m = 0; m < S->max_members; ++m) active += S->slot_plan[m] != nullptr;
+    active -= (int)S->finished.size();           // members still stepping
     if (active > 0) {
         RTM_CUDA(cudaEventRecord(S->ev0, S->stream));
         RTM_CUDA(cudaGraphLaunch(S->gexec, S->stream));
         RTM_CUDA(cudaEventRecord(S->ev1, S->stream));
         S->launches += 3LL * S->steps_per_launch;
     }
+    // the members that finished in the previous replay, harvested while this one runs
+    const bool freed = !S->finished.empty();
+    for (int m : S->finished) RTM_TRY(harvest(S, m));
+    S->finished.clear();
     // admission in arrival order among the requests whose inputs are ready (a request whose
     // seismogram is still being decoded is passed over; one that does not fit blocks the
     // rest), for as long as the replay runs: one request at least, then while the host time
@@ -506,16 +516,14 @@ int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
         unsigned flags[2] = {0, 0};
         RTM_CUDA(cudaMemcpy(flags, S->d_done, sizeof flags, cudaMemcpyDeviceToHost));
         if (flags[1]) return fail(RTM_ERR_TIMEOUT, "a batched tile load timed out");
-        bool freed = false;
         for (int m = 0; m < S->max_members; ++m)
-            if (S->slot_plan[m] && S->h_state[m].x == 3) {
-                RTM_TRY(harvest(S, m));
-                freed = true;
-            }
-        if (freed) {
-            rebuild_index(S);
-            RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
-        }
+            if (S->slot_plan[m] && S->h_state[m].x == 3) S->finished.push_back(m);
+    }
+    // slots freed by this call's harvests leave the work lists before the next replay (an
+    // activation above has already rebuilt them)
+    if (freed && !admitted) {
+        rebuild_index(S);
+        RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
     }
     if (n_active) {
         int a = 0;
