@@ -25,16 +25,6 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m)
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
 }
 
-// Number of psi quads of a member (the four strips of k_psi).
-__host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
-{
-    const int nlr = (g.dimz - 8 + 3) / 4;
-    n[0] = (g.thl - 8) * nlr;
-    n[1] = (g.dimx - 8) * ((g.thu - 8 + 3) / 4);
-    n[2] = (g.thr - 8) * nlr;
-    const int q0 = (g.dimz - g.thd + 4) & ~3;
-    n[3] = (g.dimx - 8) * ((g.dimz - 4 - q0 + 3) / 4);
-}
 
 // Slot k of a member's source-wavefield store and its scales (16-bit storage).
 template <typename T>

@@ -94,6 +94,17 @@ __host__ __device__ __forceinline__ int boundary_tiles(const Geom &g)
     return g.tiles_x * nzb + (g.nxl + (g.tiles_x - g.xr0)) * (g.tiles_z - nzb);
 }
 
+// Number of psi quads of each strip (k_psi's enumeration: left, top, right, bottom).
+__host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
+{
+    const int nlr = (g.dimz - 8 + 3) / 4;
+    n[0] = (g.thl - 8) * nlr;
+    n[1] = (g.dimx - 8) * ((g.thu - 8 + 3) / 4);
+    n[2] = (g.thr - 8) * nlr;
+    const int q0 = (g.dimz - g.thd + 4) & ~3;
+    n[3] = (g.dimx - 8) * ((g.dimz - 4 - q0 + 3) / 4);
+}
+
 __host__ __device__ __forceinline__ int ztile_origin(const Geom &g, int zt)
 {
     return zt == 0 ? 0 : g.ztop + (zt - 1) * TZ;

@@ -349,9 +349,9 @@ __device__ __forceinline__ void ring_save_quad(const Geom &g, const T *u, T *rin
     }
 }
 
-// Plain-plan psi kernel (blockIdx.y = strip).  With programmatic dependent launch it first
-// waits for the previous step kernel (whose output u_n it reads), then lets the next step
-// kernel start.  Forward with FP32 ring storage it also saves u_n's ring (slot n): done here,
+// Plain-plan psi kernel (the four strips' quads as one list).  With programmatic dependent
+// launch it first waits for the previous step kernel (whose output u_n it reads), then lets
+// the next step kernel start.  Forward with FP32 ring storage it also saves u_n's ring (slot n): done here,
 // on the strip quads, instead of inside the step kernel's boundary tiles (forward step 22.5 ->
 // 20.3 us on 3400 x 700).
 template <typename T>
@@ -359,13 +359,18 @@ __global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> 
 {
     griddep_wait();
     griddep_launch();
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!a.ring_only) {
-        T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
-        const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
-        psi_quad<T>(a.g, a.h1, a.u, psi, prof, blockIdx.y, idx, false);
+    int cnt[4];
+    psi_counts(a.g, cnt);
+    const int n = cnt[0] + cnt[1] + cnt[2] + cnt[3];
+    T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
+    const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
+    // the four strips' quads as one list (left, top, right, bottom), grid-stride
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        int lq = q, strip = 0;
+        while (strip < 3 && lq >= cnt[strip]) lq -= cnt[strip++];
+        if (!a.ring_only) psi_quad<T>(a.g, a.h1, a.u, psi, prof, strip, lq, false);
+        if (a.ring) ring_save_quad<T>(a.g, a.u, a.ring, strip, lq);
     }
-    if (a.ring) ring_save_quad<T>(a.g, a.u, a.ring, blockIdx.y, idx);
 }
 
 #include "rtm_march.cuh"
@@ -564,19 +569,24 @@ cudaError_t launch_step(int backward, const StepMaps &maps, const StepArgs<T> &a
     return cudaErrorInvalidValue;
 }
 
+// psi CTAs per SM at most (grid-stride beyond): the step kernel that follows needs the SMs
+constexpr int kPsiCtasPerSm = 4;
+
 template <typename T>
 cudaError_t launch_psi(const PsiArgs<T> &a, int pdl, cudaStream_t s)
 {
-    const Geom &g = a.g;
-    const int nlr = (g.dimz - 8 + 3) / 4;
-    int n = (g.thl - 8) * nlr;
-    n = n > (g.thr - 8) * nlr ? n : (g.thr - 8) * nlr;
-    n = n > (g.dimx - 8) * ((g.thu - 8 + 3) / 4) ? n : (g.dimx - 8) * ((g.thu - 8 + 3) / 4);
-    const int q0 = (g.dimz - g.thd + 4) & ~3;
-    const int nb = (g.dimx - 8) * ((g.dimz - 4 - q0 + 3) / 4);
-    n = n > nb ? n : nb;
+    int cnt[4];
+    psi_counts(a.g, cnt);
+    const int blocks = (cnt[0] + cnt[1] + cnt[2] + cnt[3] + 255) / 256;
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int cap = kPsiCtasPerSm * (sms > 0 ? sms : 1);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((n + 255) / 256, 4);
+    cfg.gridDim = dim3(blocks < cap ? blocks : cap);
     cfg.blockDim = dim3(256);
     cfg.stream = s;
     cudaLaunchAttribute at = pdl_attr();
