@@ -237,6 +237,11 @@ int rtm_server_step(rtm_server *server, int *n_active, int *n_queued);
  * NULL), times[3] = submit, admission, completion (seconds, monotonic clock; may be NULL). */
 int rtm_server_poll(rtm_server *server, long long *request_id, float *image, float *self_image,
                     double *times);
+/* Steps the server (rtm_server_step) until request_id has finished and returns it as
+ * rtm_server_poll does; other requests finishing meanwhile stay for rtm_server_poll.
+ * RTM_ERR_INVALID for an id never issued or already returned. */
+int rtm_server_wait(rtm_server *server, long long request_id, float *image, float *self_image,
+                    double *times);
 int rtm_server_stats(const rtm_server *server, long long *cell_updates, double *gpu_ms,
                      long long *launches, long long *bytes_in_use);
 /* CUDA-event time (ms) of the batched tile kernel on the second time step of the last

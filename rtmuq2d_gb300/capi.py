@@ -165,6 +165,7 @@ def _declare(L):
         "rtm_server_submit_zfp": (C.c_int, [vp, P, fp, fp, vp, C.c_size_t, C.c_float, C.POINTER(C.c_longlong)]),
         "rtm_server_step": (C.c_int, [vp, ip, ip]),
         "rtm_server_poll": (C.c_int, [vp, C.POINTER(C.c_longlong), fp, fp, C.POINTER(C.c_double)]),
+        "rtm_server_wait": (C.c_int, [vp, C.c_longlong, fp, fp, C.POINTER(C.c_double)]),
         "rtm_server_stats": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "rtm_server_kernel_ms": (C.c_int, [vp, C.POINTER(C.c_double)]),
@@ -198,7 +199,7 @@ def exported_symbols():
             "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
             "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_submit_zfp",
             "rtm_server_step",
-            "rtm_server_poll", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
+            "rtm_server_poll", "rtm_server_wait", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
             "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
             "rtm_zfp_encode_float2d", "rtm_routine_run", "rtm_routine_batch"]
 
@@ -502,6 +503,17 @@ class Server:
         m = p.nx * p.nz
         return (rid.value, img[:m].reshape(p.nx, p.nz).copy(), slf[:m].reshape(p.nx, p.nz).copy(),
                 tuple(times))
+
+    def wait(self, request_id: int):
+        """Steps until request_id has finished: (image, self_image, (t_submit, t_admit, t_done))."""
+        p = self.params.get(request_id)       # None: not pending here, the library refuses it
+        shape = (p.nx, p.nz) if p is not None else (0,)
+        img = np.zeros(shape, np.float32)
+        slf = np.zeros(shape, np.float32)
+        times = (C.c_double * 3)()
+        _check(lib().rtm_server_wait(self.handle, request_id, _fp(img), _fp(slf), times))
+        del self.params[request_id]
+        return img, slf, tuple(times)
 
     def stats(self) -> dict:
         cu, ms, ln, by = C.c_longlong(), C.c_double(), C.c_longlong(), C.c_longlong()

@@ -323,6 +323,20 @@ static void decoder_loop(rtm_server *S)
     }
 }
 
+// Hands a finished request to the caller and frees it.
+static int take_done(rtm_server *S, std::map<long long, ServeRequest *>::iterator it,
+                     long long *request_id, float *image, float *self_image, double *times)
+{
+    ServeRequest *R = it->second;
+    if (request_id) *request_id = R->id;
+    if (image) memcpy(image, R->img.data(), R->img.size() * sizeof(float));
+    if (self_image) memcpy(self_image, R->slf.data(), R->slf.size() * sizeof(float));
+    if (times) { times[0] = R->t_submit; times[1] = R->t_admit; times[2] = R->t_done; }
+    S->done.erase(it);
+    delete R;
+    return RTM_OK;
+}
+
 }  // namespace rtm
 
 extern "C" {
@@ -542,15 +556,29 @@ int rtm_server_poll(rtm_server *S, long long *request_id, float *image, float *s
 {
     if (!S) return fail(RTM_ERR_INVALID, "null server");
     if (S->done.empty()) return RTM_ERR_BUSY;
-    auto it = S->done.begin();
-    ServeRequest *R = it->second;
-    if (request_id) *request_id = R->id;
-    if (image) memcpy(image, R->img.data(), R->img.size() * sizeof(float));
-    if (self_image) memcpy(self_image, R->slf.data(), R->slf.size() * sizeof(float));
-    if (times) { times[0] = R->t_submit; times[1] = R->t_admit; times[2] = R->t_done; }
-    S->done.erase(it);
-    delete R;
-    return RTM_OK;
+    return take_done(S, S->done.begin(), request_id, image, self_image, times);
+}
+
+// Steps the server until request `request_id` has finished and returns it as
+// rtm_server_poll does; requests that finish meanwhile stay queued for rtm_server_poll.
+int rtm_server_wait(rtm_server *S, long long request_id, float *image, float *self_image,
+                    double *times)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null server");
+    if (request_id < 1 || request_id >= S->next_id)
+        return fail(RTM_ERR_INVALID, "unknown request %lld", request_id);
+    for (;;) {
+        auto it = S->done.find(request_id);
+        if (it != S->done.end()) return take_done(S, it, nullptr, image, self_image, times);
+        bool live = false;
+        for (const ServeRequest *R : S->queue) live |= R->id == request_id;
+        for (const ServeRequest *R : S->slot_req) live |= R && R->id == request_id;
+        if (!live) return fail(RTM_ERR_INVALID, "request %lld was already returned", request_id);
+        int active = 0;
+        RTM_TRY(rtm_server_step(S, &active, nullptr));
+        // nothing resident: the request's seismogram is still being decoded
+        if (active == 0) std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
 }
 
 // Totals since creation: credited cell-updates of finished requests, GPU milliseconds of

@@ -79,6 +79,26 @@ def test_server_mixed_batch_equals_each_alone(engine):
     assert 0.0 < kernel_ms < st["gpu_ms"]     # the tile kernel of one step, timed alone
 
 
+def test_server_wait_returns_the_named_request(engine):
+    """rtm_server_wait steps until the named request finishes (out of submission order); the
+    others finishing meanwhile stay for rtm_server_poll, and a returned id is refused."""
+    d = load()
+    cases = _mix(engine, d)[:3]
+    solo = [_alone(engine, c)[:2] for c in cases]
+    srv = engine.Server(0, max_members=2, steps_per_launch=9)
+    ids = [srv.submit(*c) for c in cases]
+    img, slf, times = srv.wait(ids[2])
+    assert np.array_equal(img, solo[2][0]) and np.array_equal(slf, solo[2][1])
+    assert times[0] <= times[1] <= times[2]
+    with pytest.raises(engine.RtmError):
+        srv.wait(ids[2])
+    rest = srv.run_all()
+    srv.close()
+    assert sorted(rest) == ids[:2]
+    for rid, (i, s) in zip(ids[:2], solo[:2]):
+        assert np.array_equal(rest[rid][0], i) and np.array_equal(rest[rid][1], s)
+
+
 def test_server_admission_respects_budget(engine):
     d = load()
     cases = [_case(engine, d, "uneven", storage=1) for _ in range(3)]
