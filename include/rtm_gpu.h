@@ -308,11 +308,14 @@ typedef struct rtm_survey {
     int shot_spacing;               /* spacingShot */
     int n_shots;                    /* numberOfShots */
     float zfp_tolerance;            /* zfp_tolerance */
+    int normalize_by_self;          /* 1: stack / self-image stack, the whole-survey branch
+                                       commented out at rtm_iso2d.c:152 (0: as the reference) */
 } rtm_survey;
 /* Runs the whole migration of one simulation: per shot a forward propagation on the GPU
  * with the shot's seismogram decoded on the host meanwhile, then the adjoint propagation;
- * the per-shot images stay in memory (no TEMPORARY_FILES) and are stacked in shot order in
- * float32 as the reference stacks them; both output files are written.  RTM_ERR_IO when an
+ * the per-shot images and self images stay in memory (no TEMPORARY_FILES) and are stacked in
+ * shot order in float32 as the reference stacks them (the image stack divided by the self-image
+ * stack when normalize_by_self is set); both output files are written.  RTM_ERR_IO when an
  * input cannot be read or an output written (the reference exits instead). */
 int rtm_routine_run(const rtm_params *p, const rtm_survey *survey, int simulation_id);
 /* rtm_routine over several simulations on one GPU (replaces the MPI fan-out of

@@ -5,8 +5,10 @@
  * Same inputs, outputs and arithmetic of the stack as the reference: velocity and wavelet
  * read raw (pi_file.c:11-32), edge-replicated into the CPML (extend_matrix), per shot a
  * forward propagation, the shot's ZFP seismogram decoded, an adjoint propagation into a
- * zeroed image and self image; images summed over shots in float32 in shot order
- * (rtm_iso2d.c:115-129), the stack written, its Laplacian (laplacian_filter2D) written.
+ * zeroed image and self image; images and self images summed over shots in float32 in shot
+ * order (rtm_iso2d.c:115-129), optionally the image stack divided by the self-image stack
+ * (the whole-survey branch the reference leaves commented out, rtm_iso2d.c:150-156), the
+ * stack written, its Laplacian (laplacian_filter2D) written.
  * Differences: the per-shot images stay in host memory instead of TEMPORARY_FILES
  * round trips (rtm_iso2d.c:95-103, 108-140), the decode runs while the GPU propagates
  * (rtm_forward_modeling returns once the forward pass is queued), and errors are returned
@@ -38,6 +40,13 @@ static int write_raw(const char *path, const float *src, size_t n)
     return (put == n && closed == 0) ? RTM_OK : RTM_ERR_IO;
 }
 
+/* rtm_iso2d.c:148-156: the whole-survey branch divides the stack by the self-image stack
+ * (commented out in the reference, which keeps the plain stack). */
+static void normalize_stack(float *stack, const float *self_stack, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) stack[i] = stack[i] / self_stack[i];
+}
+
 static int format_path(char *out, const char *pattern, int id)
 {
     if (!pattern) return RTM_ERR_INVALID;
@@ -67,9 +76,10 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     float *img = (float *)calloc(nimg, sizeof(float));
     float *slf = (float *)calloc(nimg, sizeof(float));
     float *stack = (float *)calloc(nimg, sizeof(float));
+    float *sstack = (float *)calloc(nimg, sizeof(float));
     float *lap = (float *)calloc(nimg, sizeof(float));
     char path[RTM_PATH_LEN];
-    if (!model || !ext || !wav || !seis || !img || !slf || !stack || !lap) {
+    if (!model || !ext || !wav || !seis || !img || !slf || !stack || !sstack || !lap) {
         st = RTM_ERR_NOMEM;
         goto done;
     }
@@ -94,10 +104,13 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
         memset(img, 0, nimg * sizeof(float));
         memset(slf, 0, nimg * sizeof(float));
         if ((st = rtm_adjoint_modeling(&p, simulation_id, shot, ext, wav, seis, img, slf)) != RTM_OK) goto done;
-        /* rtm_iso2d.c:121-126: float sum in shot order */
-        for (size_t i = 0; i < nimg; ++i) stack[i] = stack[i] + img[i];
+        /* rtm_iso2d.c:121-126: float sums in shot order */
+        for (size_t i = 0; i < nimg; ++i) {
+            stack[i] = stack[i] + img[i];
+            sstack[i] = sstack[i] + slf[i];
+        }
     }
-    /* rtm_iso2d.c:148-164 (the normalisation at :152 is commented out in the reference) */
+    if (s->normalize_by_self) normalize_stack(stack, sstack, nimg);
     if ((st = format_path(path, s->stacked_file, simulation_id)) != RTM_OK) goto done;
     if ((st = write_raw(path, stack, nimg)) != RTM_OK) goto done;
     if ((st = rtm_laplacian_filter2D(&p, lap, stack)) != RTM_OK) goto done;
@@ -105,7 +118,7 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     st = write_raw(path, lap, nimg);
 done:
     free(model); free(ext); free(wav); free(seis);
-    free(img); free(slf); free(stack); free(lap);
+    free(img); free(slf); free(stack); free(sstack); free(lap);
     return st;
 }
 
@@ -140,8 +153,9 @@ static int read_bytes(const char *path, unsigned char **out, size_t *n)
  * rtm_routine(simulation) out over MPI ranks (mpi_rtm_iso2d.c:39-51); here every (simulation,
  * shot) migration is a request of one rtm_server on this GPU, so the UQ realizations and
  * their shots run resident together.  Per simulation the same files and outputs as
- * rtm_routine_run: the shots' images summed in float32 in shot order (an image that finishes
- * early waits for its predecessors), the stack and its Laplacian written.  Each shot's ZFP
+ * rtm_routine_run: the shots' images and self images summed in float32 in shot order (an
+ * image that finishes early waits for its predecessors), the stack (normalised as
+ * rtm_routine_run does it) and its Laplacian written.  Each shot's ZFP
  * stream (keyed by shot id, as the reference keys it) is read once and decoded per request
  * by the server's host threads while the GPU steps.
  */
@@ -169,14 +183,17 @@ int rtm_routine_batch(const rtm_params *params, const rtm_survey *s, const int *
     float *slf = (float *)calloc(nimg, sizeof(float));
     float *lap = (float *)calloc(nimg, sizeof(float));
     float *stack = (float *)calloc(nimg * (size_t)n_simulations, sizeof(float));
+    float *sstack = (float *)calloc(nimg * (size_t)n_simulations, sizeof(float));
     unsigned char **zs = (unsigned char **)calloc(n_shots > 0 ? (size_t)n_shots : 1, sizeof(*zs));
     size_t *zb = (size_t *)calloc(n_shots > 0 ? (size_t)n_shots : 1, sizeof(*zb));
     long long *ids = (long long *)calloc(n_req > 0 ? n_req : 1, sizeof(*ids));
-    float **held = (float **)calloc(n_req > 0 ? n_req : 1, sizeof(*held));   /* finished, not yet summed */
+    /* finished, not yet summed: image then self image */
+    float **held = (float **)calloc(n_req > 0 ? n_req : 1, sizeof(*held));
     int *next_shot = (int *)calloc((size_t)n_simulations, sizeof(int));
     rtm_server *srv = NULL;
     char path[RTM_PATH_LEN];
-    if (!model || !ext || !wav || !img || !slf || !lap || !stack || !zs || !zb || !ids || !held || !next_shot) {
+    if (!model || !ext || !wav || !img || !slf || !lap || !stack || !sstack || !zs || !zb || !ids || !held ||
+        !next_shot) {
         st = RTM_ERR_NOMEM;
         goto done;
     }
@@ -209,16 +226,21 @@ int rtm_routine_batch(const rtm_params *params, const rtm_survey *s, const int *
             size_t r = 0;
             while (r < n_req && ids[r] != rid) ++r;
             if (r == n_req) { st = RTM_ERR_INVALID; goto done; }
-            held[r] = (float *)malloc(nimg * sizeof(float));
+            held[r] = (float *)malloc(2 * nimg * sizeof(float));
             if (!held[r]) { st = RTM_ERR_NOMEM; goto done; }
             memcpy(held[r], img, nimg * sizeof(float));
+            memcpy(held[r] + nimg, slf, nimg * sizeof(float));
             ++finished;
-            /* rtm_iso2d.c:121-126: float sum in shot order */
+            /* rtm_iso2d.c:121-126: float sums in shot order */
             const int i = (int)(r / (size_t)n_shots);
             float *stk = stack + (size_t)i * nimg;
+            float *sstk = sstack + (size_t)i * nimg;
             while (next_shot[i] < n_shots && held[(size_t)i * n_shots + next_shot[i]]) {
                 float *im = held[(size_t)i * n_shots + next_shot[i]];
-                for (size_t q = 0; q < nimg; ++q) stk[q] = stk[q] + im[q];
+                for (size_t q = 0; q < nimg; ++q) {
+                    stk[q] = stk[q] + im[q];
+                    sstk[q] = sstk[q] + im[nimg + q];
+                }
                 free(im);
                 held[(size_t)i * n_shots + next_shot[i]] = NULL;
                 ++next_shot[i];
@@ -227,7 +249,8 @@ int rtm_routine_batch(const rtm_params *params, const rtm_survey *s, const int *
         if (finished < n_req && active == 0 && queued == 0) { st = RTM_ERR_INVALID; goto done; }
     }
     for (int i = 0; i < n_simulations; ++i) {
-        const float *stk = stack + (size_t)i * nimg;
+        float *stk = stack + (size_t)i * nimg;
+        if (s->normalize_by_self) normalize_stack(stk, sstack + (size_t)i * nimg, nimg);
         if ((st = format_path(path, s->stacked_file, simulation_ids[i])) != RTM_OK) goto done;
         if ((st = write_raw(path, stk, nimg)) != RTM_OK) goto done;
         if ((st = rtm_laplacian_filter2D(&p, lap, stk)) != RTM_OK) goto done;
@@ -238,7 +261,7 @@ done:
     if (srv) rtm_server_destroy(srv);
     if (held) for (size_t r = 0; r < n_req; ++r) free(held[r]);
     if (zs) for (int k = 0; k < n_shots; ++k) free(zs[k]);
-    free(model); free(ext); free(wav); free(img); free(slf); free(lap); free(stack);
+    free(model); free(ext); free(wav); free(img); free(slf); free(lap); free(stack); free(sstack);
     free(zs); free(zb); free(ids); free(held); free(next_shot);
     return st;
 }

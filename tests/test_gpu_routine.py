@@ -87,3 +87,34 @@ def test_routine_batch_matches_routine_per_simulation(engine, tmp_path):
     assert rel_l2(batch[sim_id][0], d["routine/stacked"]) <= 1e-4
     assert rel_l2(batch[sim_id][1], d["routine/laplacian"]) <= 1e-4
     assert rel_l2(batch[other][0], batch[sim_id][0]) > 1e-3     # the second model differs
+
+
+@pytest.mark.parametrize("batched", (False, True))
+def test_routine_stack_normalized_by_self_image(engine, oracle, tmp_path, batched):
+    """normalize_by_self: the whole-survey branch the reference leaves commented out
+    (rtm_iso2d.c:152), the image stack divided by the self-image stack.  Checked against the
+    oracle's per-shot images and self images of the same decoded seismograms, summed in shot
+    order: stack * self_stack reproduces the image stack within the image bar (1e-4) wherever
+    the quotient is finite."""
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    s.normalize_by_self = 1
+    if batched:
+        engine.routine_batch(p, s, [sim_id], max_members=2)
+    else:
+        engine.routine_run(p, s, sim_id)
+    st, lp = _outputs(d, tmp_path, sim_id)
+    _, n_shots, first, spacing, depth = (int(v) for v in d["routine/survey"])
+    tol = float(d["routine/tol"][0])
+    img = np.zeros((p.nx, p.nz), np.float32)
+    slf = np.zeros((p.nx, p.nz), np.float32)
+    for k in range(n_shots):
+        q = p.replace(shot_x=first + k * spacing, shot_z=depth)
+        ext = oracle.extend_matrix(q.as_dict(), d["uneven/model"])
+        seis = engine.zfp_decode(d["routine/seis_%d" % (k + 1)].tobytes(), q.rec_count, q.nt, tol)
+        oi, os_ = oracle.migrate(q.as_dict(), ext, d["uneven/wavelet"], seis)
+        img = img + oi
+        slf = slf + os_
+    ok = np.isfinite(st) & (slf > 0)
+    assert ok.mean() > 0.9
+    assert rel_l2(st[ok] * slf[ok], img[ok]) <= 1e-4
+    assert rel_l2(img, d["routine/stacked"]) <= 1e-4          # the oracle's plain stack, pinned
