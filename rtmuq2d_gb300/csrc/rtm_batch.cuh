@@ -381,33 +381,42 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
     __shared__ int s_base[kMaxMembers + 1];
     __shared__ int2 s_state[kMaxMembers];
     __shared__ float red[kStripBlock / 32];
-    // The current member's descriptor (all but its tensor maps), staged by one coalesced
-    // copy per member change, so that an item's addresses come from shared memory and its
-    // data loads all issue at once.
+    // The block's member descriptor (all but its tensor maps) in shared memory, so that an
+    // item's addresses come from there and its data loads all issue at once.  Consecutive
+    // blocks of a CTA are a grid apart, mostly in other members: the next block's descriptor
+    // is copied (cp.async) into the other buffer while this block's items run.
     constexpr int kMapBytes = (int)offsetof(BMember<T>, g);
     static_assert(kMapBytes % 16 == 0 && sizeof(BMember<T>) % 16 == 0, "16-byte copy of the descriptor");
-    __shared__ __align__(64) int4 s_desc[sizeof(BMember<T>) / 16];
+    __shared__ __align__(64) int4 s_desc[2][sizeof(BMember<T>) / 16];
+    auto stage_desc = [&](int mm, int buf) {
+        const int4 *src = reinterpret_cast<const int4 *>(mem + mm);
+        for (int k = kMapBytes / 16 + threadIdx.x; k < (int)(sizeof(BMember<T>) / 16); k += blockDim.x)
+            cp_async16(&s_desc[buf][k], &src[k]);
+        cp_async_commit();
+    };
     // the next step's k_bpsi may launch; it waits for this grid to complete
     griddep_launch();
     const int nmem = ix->nmem;
     for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->corr_base[k];
     for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
-    griddep_wait();                                    // this step's tiles (and psi)
     __syncthreads();
     const int n = s_base[nmem];
-    int m = 0, m_desc = -1;
-    for (int base = blockIdx.x * kStripBlock; base < n; base += gridDim.x * kStripBlock) {
-        while (s_base[m + 1] <= base) ++m;             // block-uniform member
-        if (m != m_desc) {
-            __syncthreads();                           // the previous member's items are done
-            const int4 *src = reinterpret_cast<const int4 *>(mem + m);
-            for (int k = kMapBytes / 16 + threadIdx.x; k < (int)(sizeof(BMember<T>) / 16); k += blockDim.x)
-                s_desc[k] = src[k];
-            __syncthreads();
-            m_desc = m;
-        }
+    const int stride = gridDim.x * kStripBlock;
+    int m = 0, buf = 0;
+    if (blockIdx.x * kStripBlock < n) {
+        while (s_base[m + 1] <= blockIdx.x * kStripBlock) ++m;
+        stage_desc(m, 0);                              // descriptors do not change in a replay
+    }
+    griddep_wait();                                    // this step's tiles (and psi)
+    for (int base = blockIdx.x * kStripBlock; base < n; base += stride) {
+        int next_m = m;                                // member of the CTA's next block
+        if (base + stride < n)
+            while (s_base[next_m + 1] <= base + stride) ++next_m;
+        cp_async_wait_all();
+        __syncthreads();          // descriptor `buf` visible; the previous block is done with the other
+        if (base + stride < n) stage_desc(next_m, buf ^ 1);
         const int2 st = s_state[m];
-        const BMember<T> &M = *reinterpret_cast<const BMember<T> *>(s_desc);
+        const BMember<T> &M = *reinterpret_cast<const BMember<T> *>(s_desc[buf]);
         const Geom &g = M.g;
         const bool live = (st.x == 1 || st.x == 2) && st.y < g.nt;
         const CorrShape cs = corr_shape(g);
@@ -472,6 +481,8 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
                     store_get<T>(member_slot(M, tau + 1), M.store_prec, (size_t)r, scale);
             }
         }
+        m = next_m;
+        buf ^= 1;
     }
     // The last CTA to finish advances every active member by one step (a forward pass has
     // nt steps, a backward pass nt + 1, the last one images only), one member per thread.

@@ -133,6 +133,15 @@ __device__ __forceinline__ void ldg4(const double *p, double (&q)[4])
     const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
     q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
 }
+// 16-byte asynchronous copy global -> shared (cp.async), its group commit and wait.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void st4(float *p, const float (&q)[4])
 {
     *reinterpret_cast<float4 *>(p) = make_float4(q[0], q[1], q[2], q[3]);
