@@ -1189,6 +1189,8 @@ int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wa
                      const float *seismogram, float *image, float *self_image)
 {
     if (!p || !velocity || !image || !self_image) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->n_wavelet > 0 && !wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
+    if (p->rec_count > 0 && !seismogram) return fail(RTM_ERR_INVALID, "null seismogram");
     rtm_plan *P = nullptr;
     RTM_TRY(acquire_plan(*p, &P));
     int st = forward_host(P, velocity, wavelet, nullptr);
@@ -1201,6 +1203,7 @@ int rtm_model_seismogram(const rtm_params *p, const float *velocity, const float
                          float *seismogram)
 {
     if (!p || !velocity || !seismogram) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->n_wavelet > 0 && !wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
     if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "host recording is FP32");
     rtm_plan *P = nullptr;
     RTM_TRY(acquire_plan(*p, &P));

@@ -180,8 +180,10 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
         P->own_stream = false;
     }
     const Geom &g = P->g;
-    if (g.tx != kBatchTileX)              // tensor-map boxes must match the kernel's tiles
+    if (g.tx != kBatchTileX) {            // tensor-map boxes must match the kernel's tiles
+        S->idle.push_back(P);
         return fail(RTM_ERR_INVALID, "batched member with tile width %d (needs %d)", g.tx, kBatchTileX);
+    }
     cudaStream_t s = S->up;
     float *stage = P->at<float>(P->L.staging);
     RTM_CUDA(cudaMemcpyAsync(stage, R->vel.data(), R->vel.size() * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -337,21 +339,9 @@ static int take_done(rtm_server *S, std::map<long long, ServeRequest *>::iterato
     return RTM_OK;
 }
 
-}  // namespace rtm
-
-extern "C" {
-
-int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per_launch,
-                      rtm_server **out)
+// Device resources, graph and decoder threads of a new server (rtm_server_create).
+static int server_init(rtm_server *S, long long hbm_budget_bytes)
 {
-    if (!out) return fail(RTM_ERR_INVALID, "null argument");
-    if (max_members < 1 || max_members > kMaxMembers)
-        return fail(RTM_ERR_INVALID, "max_members must be in [1, %d]", kMaxMembers);
-    if (steps_per_launch < 1 || steps_per_launch > 256)
-        return fail(RTM_ERR_INVALID, "steps_per_launch must be in [1, 256]");
-    std::unique_ptr<rtm_server> S(new rtm_server());
-    S->max_members = max_members;
-    S->steps_per_launch = steps_per_launch;
     if (hbm_budget_bytes <= 0) {
         size_t fr = 0, tot = 0;
         RTM_CUDA(cudaMemGetInfo(&fr, &tot));
@@ -373,54 +363,28 @@ int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per
     RTM_CUDA(cudaEventCreate(&S->kev0));
     RTM_CUDA(cudaEventCreate(&S->kev1));
     S->mem.resize(kMaxMembers);
-    S->slot_plan.assign(max_members, nullptr);
-    S->slot_req.assign(max_members, nullptr);
+    S->slot_plan.assign(S->max_members, nullptr);
+    S->slot_req.assign(S->max_members, nullptr);
     memset(&S->ix, 0, sizeof S->ix);
-    rebuild_index(S.get());
+    rebuild_index(S);
     RTM_CUDA(cudaMemcpyAsync(S->d_ix, &S->ix, sizeof S->ix, cudaMemcpyHostToDevice, S->stream));
-    RTM_TRY(capture_graph(S.get()));
+    RTM_TRY(capture_graph(S));
     RTM_CUDA(cudaStreamSynchronize(S->stream));
     const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
     const int nthreads = (int)std::min(8u, hw / 2);
-    for (int k = 0; k < nthreads; ++k) S->decoders.emplace_back(decoder_loop, S.get());
-    *out = S.release();
+    for (int k = 0; k < nthreads; ++k) S->decoders.emplace_back(decoder_loop, S);
     return RTM_OK;
 }
 
-int rtm_server_destroy(rtm_server *S)
-{
-    if (!S) return RTM_OK;
-    {
-        std::lock_guard<std::mutex> lock(S->dmu);
-        S->stopping = true;
-    }
-    S->dcv.notify_all();
-    for (auto &t : S->decoders) t.join();
-    cudaStreamSynchronize(S->up);
-    cudaStreamSynchronize(S->stream);
-    for (rtm_plan *P : S->slot_plan) if (P) plan_free(P);
-    for (rtm_plan *P : S->idle) plan_free(P);
-    for (auto *R : S->slot_req) delete R;
-    for (auto *R : S->queue) delete R;
-    for (auto &kv : S->done) delete kv.second;
-    if (S->gexec) cudaGraphExecDestroy(S->gexec);
-    cudaFree(S->d_ix); cudaFree(S->d_mem); cudaFree(S->d_state); cudaFree(S->d_done);
-    cudaFreeHost(S->h_state);
-    cudaEventDestroy(S->ev0); cudaEventDestroy(S->ev1);
-    cudaEventDestroy(S->kev0); cudaEventDestroy(S->kev1);
-    cudaEventDestroy(S->up_ev);
-    cudaStreamDestroy(S->up);
-    cudaStreamDestroy(S->stream);
-    delete S;
-    return RTM_OK;
-}
-
-int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
-                      const float *seismogram, long long *request_id)
+// rtm_server_submit; with `zfp`, the seismogram comes later from a decoder thread.
+static int submit_request(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
+                          const float *seismogram, bool zfp, long long *request_id)
 {
     if (!S || !p || !velocity) return fail(RTM_ERR_INVALID, "null argument");
     RTM_TRY(check_params(*p));
     if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "the server runs FP32 migrations");
+    if (p->n_wavelet > 0 && !wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
+    if (p->rec_count > 0 && !seismogram && !zfp) return fail(RTM_ERR_INVALID, "null seismogram");
     rtm_params q = *p;
     q.tile_x = kBatchTileX;
     const long long bytes = (long long)make_layout(q, make_geom(q, true)).total;
@@ -440,6 +404,63 @@ int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity,
     return RTM_OK;
 }
 
+}  // namespace rtm
+
+extern "C" {
+
+int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per_launch,
+                      rtm_server **out)
+{
+    if (!out) return fail(RTM_ERR_INVALID, "null argument");
+    if (max_members < 1 || max_members > kMaxMembers)
+        return fail(RTM_ERR_INVALID, "max_members must be in [1, %d]", kMaxMembers);
+    if (steps_per_launch < 1 || steps_per_launch > 256)
+        return fail(RTM_ERR_INVALID, "steps_per_launch must be in [1, 256]");
+    rtm_server *S = new rtm_server();
+    S->max_members = max_members;
+    S->steps_per_launch = steps_per_launch;
+    const int st = server_init(S, hbm_budget_bytes);
+    if (st != RTM_OK) {
+        rtm_server_destroy(S);            // releases what was created before the failure
+        return st;
+    }
+    *out = S;
+    return RTM_OK;
+}
+
+int rtm_server_destroy(rtm_server *S)
+{
+    if (!S) return RTM_OK;
+    {
+        std::lock_guard<std::mutex> lock(S->dmu);
+        S->stopping = true;
+    }
+    S->dcv.notify_all();
+    for (auto &t : S->decoders) t.join();
+    if (S->up) cudaStreamSynchronize(S->up);
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    for (rtm_plan *P : S->slot_plan) if (P) plan_free(P);
+    for (rtm_plan *P : S->idle) plan_free(P);
+    for (auto *R : S->slot_req) delete R;
+    for (auto *R : S->queue) delete R;
+    for (auto &kv : S->done) delete kv.second;
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    cudaFree(S->d_ix); cudaFree(S->d_mem); cudaFree(S->d_state); cudaFree(S->d_done);
+    if (S->h_state) cudaFreeHost(S->h_state);
+    for (cudaEvent_t e : {S->ev0, S->ev1, S->kev0, S->kev1, S->up_ev})
+        if (e) cudaEventDestroy(e);
+    if (S->up) cudaStreamDestroy(S->up);
+    if (S->stream) cudaStreamDestroy(S->stream);
+    delete S;
+    return RTM_OK;
+}
+
+int rtm_server_submit(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
+                      const float *seismogram, long long *request_id)
+{
+    return submit_request(S, p, velocity, wavelet, seismogram, false, request_id);
+}
+
 // As rtm_server_submit, with the seismogram as a ZFP fixed-accuracy stream (what
 // zfp2d_lossyCompression writes, tolerance `tol`): a host decoder thread decodes it while
 // the GPU steps; the request is admitted once decoded.
@@ -448,7 +469,7 @@ int rtm_server_submit_zfp(rtm_server *S, const rtm_params *p, const float *veloc
 {
     if (!S || !p || !velocity || (!zfp_stream && zfp_bytes)) return fail(RTM_ERR_INVALID, "null argument");
     long long id = 0;
-    RTM_TRY(rtm_server_submit(S, p, velocity, wavelet, nullptr, &id));
+    RTM_TRY(submit_request(S, p, velocity, wavelet, nullptr, true, &id));
     ServeRequest *R = S->queue.back();
     R->zfp.assign(static_cast<const unsigned char *>(zfp_stream),
                   static_cast<const unsigned char *>(zfp_stream) + zfp_bytes);

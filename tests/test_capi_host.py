@@ -44,6 +44,27 @@ def test_params_check_rejects_bad_configurations(engine):
     params_check(q.replace(storage=0))
 
 
+def test_entry_points_reject_missing_inputs(engine):
+    """Null inputs are refused with RTM_ERR_INVALID before any device work."""
+    import ctypes as C
+    from rtmuq2d_gb300 import capi, workloads
+    p = workloads.params_tiny()
+    lib = capi.lib()
+    vel = np.ones((p.dim_x, p.dim_z), np.float32)
+    wav = np.ones(p.n_wavelet, np.float32)
+    seis = np.zeros((p.rec_count, p.nt), np.float32)
+    img = np.zeros((p.nx, p.nz), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    inv = capi.RTM_ERR_INVALID
+    assert lib.rtm_migrate_shot(C.byref(p), fp(vel), None, fp(seis), fp(img), fp(img)) == inv
+    assert lib.rtm_migrate_shot(C.byref(p), fp(vel), fp(wav), None, fp(img), fp(img)) == inv
+    assert lib.rtm_migrate_shot(C.byref(p), None, fp(wav), fp(seis), fp(img), fp(img)) == inv
+    assert lib.rtm_model_seismogram(C.byref(p), fp(vel), None, fp(seis)) == inv
+    rid = C.c_longlong()
+    assert lib.rtm_server_submit(None, C.byref(p), fp(vel), fp(wav), fp(seis), C.byref(rid)) == inv
+    assert lib.rtm_server_wait(None, 1, None, None, None) == inv
+
+
 def test_footprint_accounts_for_storage(engine):
     from rtmuq2d_gb300 import workloads
     from rtmuq2d_gb300.capi import footprint_bytes

@@ -128,6 +128,31 @@ def test_server_admission_respects_budget(engine):
     srv.close()
 
 
+def test_server_rejects_missing_inputs(engine):
+    """A request without its wavelet (n_wavelet > 0) or its seismogram (rec_count > 0) is
+    refused at submission, not migrated from whatever the staging buffer holds."""
+    import ctypes as C
+    from rtmuq2d_gb300 import capi
+    d = load()
+    p, ext, wav, seis = _case(engine, d, "uneven", storage=1)
+    srv = engine.Server(0, max_members=2, steps_per_launch=8)
+    lib = capi.lib()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    rid = C.c_longlong()
+    ext = np.ascontiguousarray(ext, np.float32)
+    wav = np.ascontiguousarray(wav, np.float32)
+    seis = np.ascontiguousarray(seis, np.float32)
+    assert lib.rtm_server_submit(srv.handle, C.byref(p), fp(ext), None, fp(seis), C.byref(rid)) == \
+        capi.RTM_ERR_INVALID
+    assert lib.rtm_server_submit(srv.handle, C.byref(p), fp(ext), fp(wav), None, C.byref(rid)) == \
+        capi.RTM_ERR_INVALID
+    assert lib.rtm_server_submit(srv.handle, C.byref(p), fp(ext), fp(wav), fp(seis), C.byref(rid)) == 0
+    srv.params[rid.value] = p                  # what Server.submit records for poll()
+    out = srv.run_all()
+    srv.close()
+    assert list(out) == [rid.value]
+
+
 def _valid(engine, p):
     try:
         engine.params_check(p)
