@@ -24,10 +24,23 @@
 #include <tuple>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rtm_gpu.h"
 #include "rtm_internal.h"
 
 namespace rtm {
+
+// ---- tracing -----------------------------------------------------------------------------
+// An NVTX range over a host phase (forward / adjoint pass, autotuning, a server step and its
+// admissions and harvests), shown by Nsight Systems and usable as an ncu --nvtx filter; a
+// push and a pop when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // ---- errors ------------------------------------------------------------------------------
 static thread_local std::string t_err;
@@ -599,6 +612,7 @@ template <typename T>
 static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const float *d_wav,
                        T *d_seis_out)
 {
+    NvtxRange range("rtm forward pass");
     const Geom &g = P->g;
     cudaStream_t s = P->stream;
     T *u[2] = {P->at<T>(P->L.u[0]), P->at<T>(P->L.u[1])};
@@ -685,6 +699,7 @@ static int check_status(rtm_plan *P)
 template <typename T>
 static int run_adjoint(rtm_plan *P, const float *d_seis)
 {
+    NvtxRange range("rtm adjoint pass");
     if (!P->forward_done) return fail(RTM_ERR_STATE, "adjoint pass without a forward pass");
     const Geom &g = P->g;
     cudaStream_t s = P->stream;
@@ -962,6 +977,7 @@ int rtm_device_info(char *name, int name_len, int *sm_count, long long *hbm_byte
 // for each tile width the step kernel supports and keeps the fastest for this grid shape.
 int rtm_autotune(const rtm_params *p, int steps, int *best_tile_x, float *best_ms_per_step)
 {
+    NvtxRange range("rtm autotune");
     if (!p) return fail(RTM_ERR_INVALID, "null argument");
     RTM_TRY(check_params(*p));
     if (steps < 1) return fail(RTM_ERR_INVALID, "steps must be >= 1");

@@ -158,6 +158,7 @@ static void rebuild_index(rtm_server *S)
 // copy returns once its data is staged, so they are released right after.
 static int admit(rtm_server *S, int m, ServeRequest *R)
 {
+    NvtxRange range("rtm server admit");
     rtm_plan *P = nullptr;
     for (size_t i = 0; i < S->idle.size(); ++i)
         if (same_params(S->idle[i]->p, R->p)) {
@@ -242,6 +243,7 @@ static int activate(rtm_server *S)
 // overlap the replay.  The slot is free afterwards.
 static int harvest(rtm_server *S, int m)
 {
+    NvtxRange range("rtm server harvest");
     rtm_plan *P = S->slot_plan[m];
     ServeRequest *R = S->slot_req[m];
     const Geom &g = P->g;
@@ -489,6 +491,7 @@ int rtm_server_submit_zfp(rtm_server *S, const rtm_params *p, const float *veloc
 // finished members.
 int rtm_server_step(rtm_server *S, int *n_active, int *n_queued)
 {
+    NvtxRange range("rtm server step");
     if (!S) return fail(RTM_ERR_INVALID, "null server");
     int active = 0;
     for (int m = 0; m < S->max_members; ++m) active += S->slot_plan[m] != nullptr;
