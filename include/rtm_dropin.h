@@ -83,6 +83,7 @@ static inline int rtm_dropin_configure_from_fixed_parameters(void)
     s.shot_spacing = spacingShot; s.n_shots = numberOfShots;
     s.zfp_tolerance = zfp_tolerance;
     s.normalize_by_self = 0;            /* rtm_iso2d.c:152 is commented out */
+    s.checkpoint_file = NULL;
     return rtm_dropin_configure(&p, &s);
 }
 #endif

@@ -310,6 +310,11 @@ typedef struct rtm_survey {
     float zfp_tolerance;            /* zfp_tolerance */
     int normalize_by_self;          /* 1: stack / self-image stack, the whole-survey branch
                                        commented out at rtm_iso2d.c:152 (0: as the reference) */
+    const char *checkpoint_file;    /* rtm_routine_run only, NULL = none: a file pattern (%d:
+                                       simulation id) holding the stacks after each finished
+                                       shot; a later run of the same simulation resumes after
+                                       the last shot it holds; removed once the outputs are
+                                       written */
 } rtm_survey;
 /* Runs the whole migration of one simulation: per shot a forward propagation on the GPU
  * with the shot's seismogram decoded on the host meanwhile, then the adjoint propagation;

@@ -88,12 +88,12 @@ class RtmSurvey(C.Structure):
                 ("seismogram_file", C.c_char_p), ("stacked_file", C.c_char_p),
                 ("laplacian_file", C.c_char_p), ("first_shot", C.c_int), ("shot_depth", C.c_int),
                 ("shot_spacing", C.c_int), ("n_shots", C.c_int), ("zfp_tolerance", C.c_float),
-                ("normalize_by_self", C.c_int)]
+                ("normalize_by_self", C.c_int), ("checkpoint_file", C.c_char_p)]
 
     @classmethod
     def make(cls, velocity_file, wavelet_file, seismogram_file, stacked_file, laplacian_file,
              first_shot, shot_depth, shot_spacing=0, n_shots=1, zfp_tolerance=0.0,
-             normalize_by_self=0) -> "RtmSurvey":
+             normalize_by_self=0, checkpoint_file=None) -> "RtmSurvey":
         s = cls()
         s._keep = [x.encode() for x in (velocity_file, wavelet_file, seismogram_file, stacked_file,
                                          laplacian_file)]
@@ -102,6 +102,9 @@ class RtmSurvey(C.Structure):
         s.first_shot, s.shot_depth, s.shot_spacing = first_shot, shot_depth, shot_spacing
         s.n_shots, s.zfp_tolerance = n_shots, zfp_tolerance
         s.normalize_by_self = normalize_by_self
+        if checkpoint_file is not None:
+            s._keep.append(checkpoint_file.encode())
+            s.checkpoint_file = s._keep[-1]
         return s
 
 

@@ -11,8 +11,9 @@
  * stack written, its Laplacian (laplacian_filter2D) written.
  * Differences: the per-shot images stay in host memory instead of TEMPORARY_FILES
  * round trips (rtm_iso2d.c:95-103, 108-140), the decode runs while the GPU propagates
- * (rtm_forward_modeling returns once the forward pass is queued), and errors are returned
- * (RTM_ERR_IO) where the reference exits.
+ * (rtm_forward_modeling returns once the forward pass is queued), errors are returned
+ * (RTM_ERR_IO) where the reference exits, and, with a checkpoint file, the stacks are saved
+ * after each shot so that a run stopped by a failure resumes after its last finished shot.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -38,6 +39,52 @@ static int write_raw(const char *path, const float *src, size_t n)
     const size_t put = fwrite(src, sizeof(float), n, f);
     const int closed = fclose(f);
     return (put == n && closed == 0) ? RTM_OK : RTM_ERR_IO;
+}
+
+/* Checkpoint of a simulation's shot stack: "RTMCKPT1", int32 simulation id, nx, nz, n_shots,
+ * shots done, then the image stack and the self-image stack (float32, nx * nz each).  Written
+ * to `path`.tmp and renamed over `path`, so a reader sees a whole file or the previous one. */
+static const char kCkptMagic[8] = {'R', 'T', 'M', 'C', 'K', 'P', 'T', '1'};
+
+static int ckpt_write(const char *path, int sim, int nx, int nz, int n_shots, int done,
+                      const float *stack, const float *sstack, size_t n)
+{
+    char tmp[RTM_PATH_LEN + 8];
+    const int len = snprintf(tmp, sizeof tmp, "%s.tmp", path);
+    if (len < 0 || len >= (int)sizeof tmp) return RTM_ERR_INVALID;
+    FILE *f = fopen(tmp, "wb");
+    if (!f) return RTM_ERR_IO;
+    const int hdr[5] = {sim, nx, nz, n_shots, done};
+    int ok = fwrite(kCkptMagic, 1, 8, f) == 8 && fwrite(hdr, sizeof(int), 5, f) == 5 &&
+             fwrite(stack, sizeof(float), n, f) == n && fwrite(sstack, sizeof(float), n, f) == n;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp, path) != 0) {
+        remove(tmp);
+        return RTM_ERR_IO;
+    }
+    return RTM_OK;
+}
+
+/* Shots already stacked by a matching checkpoint (0: none, or one of another run). */
+static int ckpt_read(const char *path, int sim, int nx, int nz, int n_shots, float *stack,
+                     float *sstack, size_t n)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) return 0;
+    char magic[8];
+    int hdr[5];
+    int done = 0;
+    if (fread(magic, 1, 8, f) == 8 && memcmp(magic, kCkptMagic, 8) == 0 &&
+        fread(hdr, sizeof(int), 5, f) == 5 && hdr[0] == sim && hdr[1] == nx && hdr[2] == nz &&
+        hdr[3] == n_shots && hdr[4] > 0 && hdr[4] <= n_shots &&
+        fread(stack, sizeof(float), n, f) == n && fread(sstack, sizeof(float), n, f) == n)
+        done = hdr[4];
+    fclose(f);
+    if (!done) {                          /* not ours: start from zero stacks */
+        memset(stack, 0, n * sizeof(float));
+        memset(sstack, 0, n * sizeof(float));
+    }
+    return done;
 }
 
 /* rtm_iso2d.c:148-156: the whole-survey branch divides the stack by the self-image stack
@@ -78,10 +125,15 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     float *stack = (float *)calloc(nimg, sizeof(float));
     float *sstack = (float *)calloc(nimg, sizeof(float));
     float *lap = (float *)calloc(nimg, sizeof(float));
-    char path[RTM_PATH_LEN];
+    char path[RTM_PATH_LEN], ckpt[RTM_PATH_LEN];
+    int first_shot = 1;
     if (!model || !ext || !wav || !seis || !img || !slf || !stack || !sstack || !lap) {
         st = RTM_ERR_NOMEM;
         goto done;
+    }
+    if (s->checkpoint_file) {             /* resume after the shots a checkpoint holds */
+        if ((st = format_path(ckpt, s->checkpoint_file, simulation_id)) != RTM_OK) goto done;
+        first_shot = 1 + ckpt_read(ckpt, simulation_id, p.nx, p.nz, s->n_shots, stack, sstack, nimg);
     }
     /* rtm_iso2d.c:70-75 */
     if ((st = format_path(path, s->velocity_file, simulation_id)) != RTM_OK) goto done;
@@ -90,7 +142,7 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     rtm_extend_matrix(&p, ext, model);
 
     /* rtm_iso2d.c:77-104: shots in an arithmetic progression */
-    for (int shot_id = 1; shot_id <= s->n_shots; ++shot_id) {
+    for (int shot_id = first_shot; shot_id <= s->n_shots; ++shot_id) {
         int shot[2];
         shot[0] = s->first_shot + (shot_id - 1) * s->shot_spacing;
         shot[1] = s->shot_depth;
@@ -109,6 +161,9 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
             stack[i] = stack[i] + img[i];
             sstack[i] = sstack[i] + slf[i];
         }
+        if (s->checkpoint_file &&
+            (st = ckpt_write(ckpt, simulation_id, p.nx, p.nz, s->n_shots, shot_id, stack, sstack, nimg)) != RTM_OK)
+            goto done;
     }
     if (s->normalize_by_self) normalize_stack(stack, sstack, nimg);
     if ((st = format_path(path, s->stacked_file, simulation_id)) != RTM_OK) goto done;
@@ -116,6 +171,7 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     if ((st = rtm_laplacian_filter2D(&p, lap, stack)) != RTM_OK) goto done;
     if ((st = format_path(path, s->laplacian_file, simulation_id)) != RTM_OK) goto done;
     st = write_raw(path, lap, nimg);
+    if (st == RTM_OK && s->checkpoint_file) remove(ckpt);   /* the outputs hold the result */
 done:
     free(model); free(ext); free(wav); free(seis);
     free(img); free(slf); free(stack); free(sstack); free(lap);

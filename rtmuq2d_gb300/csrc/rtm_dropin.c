@@ -17,7 +17,7 @@
 
 static rtm_params g_p;
 static rtm_survey g_s;
-static char g_paths[5][DROPIN_PATH_LEN];
+static char g_paths[6][DROPIN_PATH_LEN];
 static int g_configured = 0;
 
 static void die(const char *what)
@@ -52,6 +52,7 @@ int rtm_dropin_configure(const rtm_params *p, const rtm_survey *survey)
     g_s.seismogram_file = keep(2, survey->seismogram_file);
     g_s.stacked_file = keep(3, survey->stacked_file);
     g_s.laplacian_file = keep(4, survey->laplacian_file);
+    g_s.checkpoint_file = keep(5, survey->checkpoint_file);
     g_configured = 1;
     return RTM_OK;
 }

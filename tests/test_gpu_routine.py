@@ -118,3 +118,35 @@ def test_routine_stack_normalized_by_self_image(engine, oracle, tmp_path, batche
     assert ok.mean() > 0.9
     assert rel_l2(st[ok] * slf[ok], img[ok]) <= 1e-4
     assert rel_l2(img, d["routine/stacked"]) <= 1e-4          # the oracle's plain stack, pinned
+
+
+def test_routine_resumes_from_its_checkpoint(engine, tmp_path):
+    """With a checkpoint file, a run that fails at shot 2 (its seismogram missing) keeps the
+    stacks of shot 1; the rerun resumes at shot 2 -- shot 1's seismogram is gone by then, so
+    it cannot have run it again -- and writes the same files, bit for bit, as an uninterrupted
+    run (the same float sums in shot order); the checkpoint is removed afterwards."""
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    engine.routine_run(p, s, sim_id)
+    want = _outputs(d, tmp_path, sim_id)
+    for f in (tmp_path / "OUTPUTS").iterdir():
+        f.unlink()
+    ck = tmp_path / "OUTPUTS" / "stack_%05d.ckpt"
+    s2 = engine.RtmSurvey.make(*(getattr(s, k).decode() for k in ("velocity_file", "wavelet_file",
+                                                                    "seismogram_file", "stacked_file",
+                                                                    "laplacian_file")),
+                               first_shot=s.first_shot, shot_depth=s.shot_depth,
+                               shot_spacing=s.shot_spacing, n_shots=s.n_shots,
+                               zfp_tolerance=s.zfp_tolerance, checkpoint_file=str(ck))
+    seis2 = tmp_path / "INPUTS" / "seismogram_00002.zfp"
+    hidden = tmp_path / "seismogram_00002.zfp"
+    seis2.rename(hidden)
+    with pytest.raises(engine.RtmError):
+        engine.routine_run(p, s2, sim_id)
+    ckpt = tmp_path / "OUTPUTS" / ("stack_%05d.ckpt" % sim_id)
+    assert ckpt.exists()
+    hidden.rename(seis2)
+    (tmp_path / "INPUTS" / "seismogram_00001.zfp").unlink()
+    engine.routine_run(p, s2, sim_id)
+    got = _outputs(d, tmp_path, sim_id)
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    assert not ckpt.exists()
