@@ -1,6 +1,6 @@
 #!/usr/bin/env bash
 # Build the oracle (CPU restatement, test infrastructure) into oracle/_build/:
-#   liboracle.so       -O2 -ffp-contract=off : the checker (matches the reference bit for bit)
+#   liboracle.so       -O2 -ffp-contract=off : the parity reference (matches the reference bit for bit)
 #   liboracle_fast.so  -O3, FMA contraction on : the timed CPU baseline ("port")
 # Plain gcc + OpenMP; builds the same on x86-64 and aarch64.
 set -euo pipefail

@@ -1,7 +1,7 @@
 /*
  * rtm_oracle.c -- CPU restatement of rtmUq2D's migration path (TEST INFRASTRUCTURE).
  *
- * This file is the oracle: the checker for the CUDA engine and the timed CPU
+ * This file is the oracle: what the CUDA engine's results are compared with, and the timed CPU
  * baseline.  It is never part of the product library.  See rtm_oracle.h for the
  * routine-by-routine map to the reference sources.
  */

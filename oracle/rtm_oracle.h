@@ -1,7 +1,7 @@
 /*
  * rtm_oracle.h -- CPU restatement of rtmUq2D's migration path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA engine is compared
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA engine is compared
  * against, and the timed CPU baseline ("port").  The product library never
  * links, loads or calls it; only tests/, __graft_entry__.smoke() and bench.py's
  * CPU-baseline leg do.
