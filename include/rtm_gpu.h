@@ -316,8 +316,8 @@ typedef struct rtm_survey {
                                        the last shot it holds; removed once the outputs are
                                        written */
 } rtm_survey;
-/* Runs the whole migration of one simulation: per shot a forward propagation on the GPU
- * with the shot's seismogram decoded on the host meanwhile, then the adjoint propagation;
+/* Runs the whole migration of one simulation: per shot a forward propagation on the GPU,
+ * then the adjoint propagation with the shot's seismogram, which host threads decode ahead;
  * the per-shot images and self images stay in memory (no TEMPORARY_FILES) and are stacked in
  * shot order in float32 as the reference stacks them (the image stack divided by the self-image
  * stack when normalize_by_self is set); both output files are written.  RTM_ERR_IO when an

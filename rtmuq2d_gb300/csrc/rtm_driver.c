@@ -10,11 +10,12 @@
  * (the whole-survey branch the reference leaves commented out, rtm_iso2d.c:150-156), the
  * stack written, its Laplacian (laplacian_filter2D) written.
  * Differences: the per-shot images stay in host memory instead of TEMPORARY_FILES
- * round trips (rtm_iso2d.c:95-103, 108-140), the decode runs while the GPU propagates
- * (rtm_forward_modeling returns once the forward pass is queued), errors are returned
+ * round trips (rtm_iso2d.c:95-103, 108-140), the seismograms are decoded ahead on host
+ * threads while the GPU migrates earlier shots, errors are returned
  * (RTM_ERR_IO) where the reference exits, and, with a checkpoint file, the stacks are saved
  * after each shot so that a run stopped by a failure resumes after its last finished shot.
  */
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -101,6 +102,68 @@ static int format_path(char *out, const char *pattern, int id)
     return (n < 0 || n >= RTM_PATH_LEN) ? RTM_ERR_INVALID : RTM_OK;
 }
 
+/* ---- seismogram decode ahead of the migrations ------------------------------------------
+ * A ZFP fixed-accuracy stream decodes serially (no block offsets), at about a hundred MB/s
+ * on one host core: longer than a full-size shot takes on the GPU.  A few threads decode
+ * the next shots' streams (at most `ahead` beyond the one being migrated) while the GPU
+ * migrates the current one; the driver takes them in shot order. */
+typedef struct {
+    const rtm_params *p;
+    const rtm_survey *s;
+    int last;               /* last shot id */
+    int ahead;              /* shots decoded beyond the one consumed */
+    size_t nseis;
+    float **buf;            /* per shot id: decoded seismogram (owned until taken) */
+    int *st;                /* per shot id: 0 pending, else RTM status + 1 */
+    int next;               /* next shot id to decode */
+    int consumed;           /* shots taken by the driver */
+    int stop;
+    pthread_mutex_t mu;
+    pthread_cond_t cv;
+} decode_ahead;
+
+static void *decode_worker(void *arg)
+{
+    decode_ahead *d = (decode_ahead *)arg;
+    char path[RTM_PATH_LEN];
+    pthread_mutex_lock(&d->mu);
+    for (;;) {
+        while (!d->stop && d->next <= d->last && d->next > d->consumed + d->ahead)
+            pthread_cond_wait(&d->cv, &d->mu);
+        if (d->stop || d->next > d->last) break;
+        const int shot = d->next++;
+        pthread_mutex_unlock(&d->mu);
+        float *b = (float *)malloc((d->nseis > 0 ? d->nseis : 1) * sizeof(float));
+        int st = b ? format_path(path, d->s->seismogram_file, shot) : RTM_ERR_NOMEM;
+        if (st == RTM_OK && d->nseis > 0)
+            st = rtm_zfp_decode_file(path, b, d->p->rec_count, d->p->nt, d->s->zfp_tolerance);
+        pthread_mutex_lock(&d->mu);
+        d->buf[shot] = b;
+        d->st[shot] = st + 1;
+        pthread_cond_broadcast(&d->cv);
+    }
+    pthread_mutex_unlock(&d->mu);
+    return NULL;
+}
+
+/* The decoded seismogram of `shot` (the caller frees it), or NULL with *status set. */
+static float *decode_take(decode_ahead *d, int shot, int *status)
+{
+    pthread_mutex_lock(&d->mu);
+    while (d->st[shot] == 0) pthread_cond_wait(&d->cv, &d->mu);
+    float *b = d->buf[shot];
+    d->buf[shot] = NULL;
+    *status = d->st[shot] - 1;
+    d->consumed = shot;
+    pthread_cond_broadcast(&d->cv);
+    pthread_mutex_unlock(&d->mu);
+    if (*status != RTM_OK) {
+        free(b);
+        return NULL;
+    }
+    return b;
+}
+
 int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulation_id)
 {
     if (!params || !s || !s->velocity_file || !s->wavelet_file || !s->seismogram_file ||
@@ -119,7 +182,7 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     float *model = (float *)calloc(nimg, sizeof(float));
     float *ext = (float *)calloc(next, sizeof(float));
     float *wav = (float *)calloc(nwav, sizeof(float));
-    float *seis = (float *)calloc(nseis > 0 ? nseis : 1, sizeof(float));
+    float *seis = NULL;
     float *img = (float *)calloc(nimg, sizeof(float));
     float *slf = (float *)calloc(nimg, sizeof(float));
     float *stack = (float *)calloc(nimg, sizeof(float));
@@ -127,13 +190,35 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     float *lap = (float *)calloc(nimg, sizeof(float));
     char path[RTM_PATH_LEN], ckpt[RTM_PATH_LEN];
     int first_shot = 1;
-    if (!model || !ext || !wav || !seis || !img || !slf || !stack || !sstack || !lap) {
+    decode_ahead dec;
+    pthread_t workers[4];
+    int nworkers = 0;
+    memset(&dec, 0, sizeof dec);
+    pthread_mutex_init(&dec.mu, NULL);
+    pthread_cond_init(&dec.cv, NULL);
+    dec.buf = (float **)calloc((size_t)s->n_shots + 1, sizeof(float *));
+    dec.st = (int *)calloc((size_t)s->n_shots + 1, sizeof(int));
+    if (!model || !ext || !wav || !img || !slf || !stack || !sstack || !lap || !dec.buf || !dec.st) {
         st = RTM_ERR_NOMEM;
         goto done;
     }
     if (s->checkpoint_file) {             /* resume after the shots a checkpoint holds */
         if ((st = format_path(ckpt, s->checkpoint_file, simulation_id)) != RTM_OK) goto done;
         first_shot = 1 + ckpt_read(ckpt, simulation_id, p.nx, p.nz, s->n_shots, stack, sstack, nimg);
+    }
+    /* the shots' seismograms decode ahead on up to four host threads */
+    dec.p = &p;
+    dec.s = s;
+    dec.last = s->n_shots;
+    dec.nseis = nseis;
+    dec.next = first_shot;
+    dec.consumed = first_shot - 1;
+    dec.ahead = s->n_shots - first_shot + 1 < 4 ? s->n_shots - first_shot + 1 : 4;
+    for (int k = 0; k < dec.ahead; ++k)
+        if (pthread_create(&workers[nworkers], NULL, decode_worker, &dec) == 0) ++nworkers;
+    if (dec.ahead > 0 && nworkers == 0) {
+        st = RTM_ERR_NOMEM;
+        goto done;
     }
     /* rtm_iso2d.c:70-75 */
     if ((st = format_path(path, s->velocity_file, simulation_id)) != RTM_OK) goto done;
@@ -149,10 +234,9 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
         p.shot_x = shot[0];
         p.shot_z = shot[1];
         if ((st = rtm_forward_modeling(&p, simulation_id, shot, ext, wav)) != RTM_OK) goto done;
-        /* the decode overlaps the queued forward propagation */
-        if ((st = format_path(path, s->seismogram_file, shot_id)) != RTM_OK) goto done;
-        if (nseis > 0 && (st = rtm_zfp_decode_file(path, seis, p.rec_count, p.nt, s->zfp_tolerance)) != RTM_OK)
-            goto done;
+        /* decoded meanwhile (or before) by the decode-ahead threads */
+        free(seis);
+        if (!(seis = decode_take(&dec, shot_id, &st))) goto done;
         memset(img, 0, nimg * sizeof(float));
         memset(slf, 0, nimg * sizeof(float));
         if ((st = rtm_adjoint_modeling(&p, simulation_id, shot, ext, wav, seis, img, slf)) != RTM_OK) goto done;
@@ -173,6 +257,16 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     st = write_raw(path, lap, nimg);
     if (st == RTM_OK && s->checkpoint_file) remove(ckpt);   /* the outputs hold the result */
 done:
+    pthread_mutex_lock(&dec.mu);
+    dec.stop = 1;
+    pthread_cond_broadcast(&dec.cv);
+    pthread_mutex_unlock(&dec.mu);
+    for (int k = 0; k < nworkers; ++k) pthread_join(workers[k], NULL);
+    if (dec.buf)
+        for (int k = 0; k <= s->n_shots; ++k) free(dec.buf[k]);
+    free(dec.buf); free(dec.st);
+    pthread_cond_destroy(&dec.cv);
+    pthread_mutex_destroy(&dec.mu);
     free(model); free(ext); free(wav); free(seis);
     free(img); free(slf); free(stack); free(sstack); free(lap);
     return st;

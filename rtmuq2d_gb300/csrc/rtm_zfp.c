@@ -44,6 +44,21 @@ typedef struct {
 
 static void zr_fill(zreader *r)
 {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__
+    if (r->end - r->p >= 8) {             /* whole bytes up to 57..64 valid bits, one load */
+        uint64_t w;
+        memcpy(&w, r->p, 8);
+        const unsigned k = (64 - r->n) >> 3;
+        if (k == 8) {
+            r->buf = w;
+        } else {
+            r->buf |= (w & ((UINT64_C(1) << (8 * k)) - 1)) << r->n;
+        }
+        r->p += k;
+        r->n += 8 * k;
+        return;
+    }
+#endif
     while (r->n <= 56) {
         uint64_t byte = 0;
         if (r->p < r->end) byte = *r->p++;
@@ -71,6 +86,13 @@ static uint64_t zr_bits(zreader *r, unsigned m)
     r->buf >>= m;
     r->n -= m;
     return v;
+}
+
+/* Drops m <= n buffered bits. */
+static void zr_skip(zreader *r, unsigned m)
+{
+    r->buf = m < 64 ? r->buf >> m : 0;
+    r->n -= m;
 }
 
 /* bits consumed beyond the stream's end (the stream was truncated or corrupt) */
@@ -133,12 +155,27 @@ static void decode_block_f2(zreader *r, int minexp, float out[16])
     for (unsigned k = 32; k-- > kmin;) {
         uint64_t x = zr_bits(r, n);         /* plane k of the first n coefficients */
         while (n < 16 && zr_bit(r)) {       /* group test: one more becomes significant */
-            while (n < 15 && !zr_bit(r)) ++n;
+            if (n < 15) {
+                /* a run of zeros ends at the next significant coefficient, or at the 15th
+                 * after which the last one is implied: count the run in one step */
+                if (r->n < 16) zr_fill(r);
+                const unsigned lim = 15 - n;
+                const unsigned z = r->buf ? (unsigned)__builtin_ctzll(r->buf) : 64u;
+                if (z >= lim) {
+                    zr_skip(r, lim);
+                    n = 15;
+                } else {
+                    zr_skip(r, z + 1);
+                    n += z;
+                }
+            }
             x |= UINT64_C(1) << n;
             ++n;
         }
-        for (unsigned i = 0; x; ++i, x >>= 1)
-            u[i] |= (uint32_t)(x & 1u) << k;
+        while (x) {                          /* set bits of the plane into the coefficients */
+            u[__builtin_ctzll(x)] |= UINT32_C(1) << k;
+            x &= x - 1;
+        }
     }
     /* negabinary -> two's complement, sequency order -> block order */
     int32_t q[16];
@@ -146,7 +183,17 @@ static void decode_block_f2(zreader *r, int minexp, float out[16])
         q[zfp_perm2[i]] = (int32_t)((u[i] ^ 0xaaaaaaaau) - 0xaaaaaaaau);
     for (int x = 0; x < 4; ++x) inv_lift4(q + x, 4);        /* along y */
     for (int y = 0; y < 4; ++y) inv_lift4(q + 4 * y, 1);    /* along x */
-    for (int i = 0; i < 16; ++i) out[i] = ldexpf((float)q[i], emax - 30);
+    /* q * 2^(emax-30): one rounding either way, so a multiply by the normal power of two
+     * equals ldexpf, which remains for scales outside the normal range */
+    const int e = emax - 30;
+    if (e >= -126 && e <= 127) {
+        const uint32_t bits = (uint32_t)(e + 127) << 23;
+        float sc;
+        memcpy(&sc, &bits, sizeof sc);
+        for (int i = 0; i < 16; ++i) out[i] = (float)q[i] * sc;
+    } else {
+        for (int i = 0; i < 16; ++i) out[i] = ldexpf((float)q[i], e);
+    }
 }
 
 /* minexp of zfp's fixed-accuracy mode for `tolerance` (0: the smallest double exponent) */
