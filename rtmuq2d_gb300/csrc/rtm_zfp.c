@@ -346,15 +346,18 @@ static void encode_block_f2(zwriter *w, int minexp, const float v[16])
         while (n < 16) {
             zw_bit(w, x != 0);               /* group test */
             if (!x) break;
-            while (n < 15) {                 /* unary scan to the next significant one */
-                const unsigned b = (unsigned)(x & 1u);
-                zw_bit(w, b);
-                if (b) break;
-                x >>= 1;
-                ++n;
+            /* unary run to the next significant coefficient: its zeros and its one, or 15 - n
+             * zeros when it is the 16th (implied), written at once */
+            const unsigned z = (unsigned)__builtin_ctzll(x);
+            if (n + z < 15) {
+                zw_bits(w, UINT64_C(1) << z, z + 1);
+                x >>= z + 1;
+                n += z + 1;
+            } else {
+                zw_bits(w, 0, 15 - n);
+                x = 0;                       /* the implied 16th was x's last bit */
+                n = 16;
             }
-            x >>= 1;
-            ++n;
         }
     }
 }
