@@ -27,10 +27,12 @@
  * decodes serially; the engine overlaps it with the GPU forward propagation.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include "rtm_gpu.h"
 
@@ -369,6 +371,68 @@ size_t rtm_zfp_encode_bound(int nx, int ny)
     return blocks * 200 + 8;                 /* < 1 + 8 + 32 * 48 bits per block, whole words */
 }
 
+/* Blocks of block rows [r0, r1) into w (the serial order within the rows). */
+static void encode_rows(zwriter *w, const float *in, int nx, int ny, int minexp, int r0, int r1)
+{
+    float blk[16];
+    for (int by = 4 * r0; by < ny && by < 4 * r1; by += 4)
+        for (int bx = 0; bx < nx; bx += 4) {
+            const int mx = nx - bx < 4 ? nx - bx : 4, my = ny - by < 4 ? ny - by : 4;
+            for (int j = 0; j < my; ++j)
+                for (int i = 0; i < mx; ++i)
+                    blk[i + 4 * j] = in[(size_t)(by + j) * (size_t)nx + (size_t)(bx + i)];
+            if (mx < 4 || my < 4) {
+                for (int j = 0; j < my; ++j) pad4(blk + 4 * j, mx, 1);
+                for (int i = 0; i < 4; ++i) pad4(blk + i, my, 4);
+            }
+            encode_block_f2(w, minexp, blk);
+        }
+}
+
+/* One thread's share of a parallel encode: its block rows into a private buffer. */
+typedef struct {
+    const float *in;
+    int nx, ny, minexp, r0, r1;
+    unsigned char *buf;
+    size_t cap;
+    uint64_t nbits;         /* bits written (before the final word flush) */
+    int full;
+} enc_chunk;
+
+static void *encode_chunk(void *arg)
+{
+    enc_chunk *c = (enc_chunk *)arg;
+    zwriter w;
+    w.p = c->buf;
+    w.end = c->buf + c->cap;
+    w.buf = 0;
+    w.n = 0;
+    w.full = 0;
+    encode_rows(&w, c->in, c->nx, c->ny, c->minexp, c->r0, c->r1);
+    c->nbits = (uint64_t)(w.p - c->buf) * 8 + w.n;
+    zw_flush(&w);
+    c->full = w.full;
+    return NULL;
+}
+
+/* Appends the first nbits bits of a chunk's buffer (LSB first) to w. */
+static void append_bits(zwriter *w, const unsigned char *src, uint64_t nbits)
+{
+    for (; nbits >= 64; nbits -= 64, src += 8) {
+        uint64_t v;
+        memcpy(&v, src, 8);
+        zw_bits(w, v & 0xffffffffu, 32);
+        zw_bits(w, v >> 32, 32);
+    }
+    if (nbits) {
+        uint64_t v = 0;
+        for (unsigned i = 0; i < 8; ++i) v |= (uint64_t)src[i] << (8 * i);
+        const unsigned m = (unsigned)nbits;
+        zw_bits(w, v & 0xffffffffu, m < 32 ? m : 32);
+        if (m > 32) zw_bits(w, v >> 32, m - 32);
+    }
+}
+
 int rtm_zfp_encode_float2d(const float *in, int nx, int ny, double tolerance, void *out,
                            size_t capacity, size_t *bytes)
 {
@@ -380,19 +444,50 @@ int rtm_zfp_encode_float2d(const float *in, int nx, int ny, double tolerance, vo
     w.n = 0;
     w.full = 0;
     const int minexp = zfp_minexp(tolerance);
-    float blk[16];
-    for (int by = 0; by < ny; by += 4)
-        for (int bx = 0; bx < nx; bx += 4) {
-            const int mx = nx - bx < 4 ? nx - bx : 4, my = ny - by < 4 ? ny - by : 4;
-            for (int j = 0; j < my; ++j)
-                for (int i = 0; i < mx; ++i)
-                    blk[i + 4 * j] = in[(size_t)(by + j) * (size_t)nx + (size_t)(bx + i)];
-            if (mx < 4 || my < 4) {
-                for (int j = 0; j < my; ++j) pad4(blk + 4 * j, mx, 1);
-                for (int i = 0; i < 4; ++i) pad4(blk + i, my, 4);
+    const int rows = (ny + 3) / 4;
+    /* Large fields: block rows in chunks on host threads, their bit streams concatenated
+     * bit for bit -- the serial stream, as ZFP's OpenMP mode also produces it. */
+    enum { kMaxThreads = 16, kRowsPerThread = 64 };
+    long ncpu = sysconf(_SC_NPROCESSORS_ONLN);
+    int nthr = rows / kRowsPerThread;
+    if (nthr > kMaxThreads) nthr = kMaxThreads;
+    if (ncpu > 0 && nthr > ncpu) nthr = (int)ncpu;
+    enc_chunk ch[kMaxThreads];
+    pthread_t th[kMaxThreads];
+    int started = 0;
+    if (nthr >= 2) {
+        for (int k = 0; k < nthr; ++k) {
+            enc_chunk *c = &ch[k];
+            c->in = in; c->nx = nx; c->ny = ny; c->minexp = minexp;
+            c->r0 = (int)((long)rows * k / nthr);
+            c->r1 = (int)((long)rows * (k + 1) / nthr);
+            c->cap = (size_t)(c->r1 - c->r0) * (size_t)((nx + 3) / 4) * 200 + 16;
+            c->buf = (unsigned char *)malloc(c->cap);
+            c->nbits = 0;
+            c->full = 0;
+            if (!c->buf) break;
+            if (pthread_create(&th[k], NULL, encode_chunk, c) != 0) {
+                free(c->buf);
+                break;
             }
-            encode_block_f2(&w, minexp, blk);
+            ++started;
         }
+        for (int k = 0; k < started; ++k) pthread_join(th[k], NULL);
+        int ok = started == nthr;
+        for (int k = 0; k < started && ok; ++k) ok = !ch[k].full;
+        if (ok)
+            for (int k = 0; k < nthr; ++k) append_bits(&w, ch[k].buf, ch[k].nbits);
+        for (int k = 0; k < started; ++k) free(ch[k].buf);
+        if (!ok) {                           /* fall back to one thread */
+            w.p = (unsigned char *)out;
+            w.buf = 0;
+            w.n = 0;
+            w.full = 0;
+            encode_rows(&w, in, nx, ny, minexp, 0, rows);
+        }
+    } else {
+        encode_rows(&w, in, nx, ny, minexp, 0, rows);
+    }
     zw_flush(&w);
     if (w.full) return RTM_ERR_INVALID;
     if (bytes) *bytes = (size_t)(w.p - (unsigned char *)out);

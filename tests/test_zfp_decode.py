@@ -118,3 +118,50 @@ def test_dropin_compression_matches_reference_stream(engine, tag, tol):
     assert n == len(ref) and buf.value
     assert C.string_at(buf.value, n) == ref
     C.CDLL(None).free(buf)
+
+
+def _large_field():
+    rng = np.random.default_rng(11)
+    nrec, nt = 700, 1500                  # 375 block rows: the threaded encoder's chunks
+    t = np.arange(nt) * 4e-4
+    x = np.arange(nrec)[:, None] * 5.0
+    f = np.zeros((nrec, nt), np.float32)
+    for t0, v in ((0.2, 1500.0), (0.4, 2200.0)):
+        tt = np.sqrt(t0 ** 2 + ((x - 1750.0) / v) ** 2)
+        f += (np.exp(-((t[None, :] - tt) * 60.0) ** 2) * np.cos((t[None, :] - tt) * 125.0)).astype(np.float32)
+    f += (rng.standard_normal(f.shape) * 1e-3).astype(np.float32)
+    f[:, :50] = 0.0                       # empty blocks
+    return f
+
+
+def test_large_field_encode_round_trip(engine):
+    """A field large enough for the threaded encoder (block rows in chunks on host threads,
+    bit streams concatenated): it decodes within the tolerance."""
+    f = _large_field()
+    for tol in (1e-4, 1e-6):
+        s = engine.zfp_encode(f, tol)
+        out = engine.zfp_decode(s, f.shape[0], f.shape[1], tol)
+        assert np.abs(out - f).max() <= tol
+
+
+def test_large_field_encode_matches_reference_library(engine):
+    """The threaded encoder writes the reference library's stream byte for byte (ZFP's OpenMP
+    mode also concatenates per-chunk streams bit for bit).  Needs the reference's own build
+    (oracle/_ref, made from the reference sources where they are present)."""
+    import ctypes as C
+    import os
+    lib = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref",
+                       "libref_rtm.so")
+    if not os.path.exists(lib):
+        pytest.skip("reference build absent")
+    ref = C.CDLL(lib)
+    ref.zfp2d_lossyCompression.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                           C.c_float]
+    ref.zfp2d_lossyCompression.restype = C.c_int
+    f = np.ascontiguousarray(_large_field())
+    for tol in (1e-4, 0.0):
+        ptr = C.c_void_p()
+        n = ref.zfp2d_lossyCompression(C.byref(ptr), f.ctypes.data_as(C.POINTER(C.c_float)), f.shape[0],
+                                       f.shape[1], C.c_float(tol))
+        assert n > 0
+        assert C.string_at(ptr.value, n) == bytes(engine.zfp_encode(f, tol)), tol
