@@ -88,3 +88,81 @@ def test_host_setup_matches_reference_fixtures(engine, name):
     prof = attenuation_profile_cpml(p)
     for k, v in prof.items():
         assert np.allclose(v, d[name + "/prof_" + k], rtol=2e-7, atol=0), k
+
+
+_FIXED = r'''
+#ifndef FIXED_PARAMETERS_H
+#define FIXED_PARAMETERS_H
+static char velocityFile[] = "./INPUTS/vp_%05d.bin";
+static char waveletFile[] = "./INPUTS/wavelet.bin";
+static char seismogramFile[] = "./INPUTS/seismogram_%05d.zfp";
+static char stackedFile[] = "./OUTPUTS/stackedBrute_%05d.bin";
+static char stackedLaplacianFile[] = "./OUTPUTS/stackedLaplacian_%05d.bin";
+static const float zfp_tolerance = 0.0001;
+static const float spacingGrid = 10.0;
+static const float sampling = 0.001;
+static const int numberOfSimulations = 1;
+static const int Nx = 37;
+static const int Nz = 29;
+static const int firstLocationShot = 18;
+static const int depthShot = 2;
+static const int spacingShot = 4;
+static const int numberOfShots = 2;
+static const int firstLocationReceiver = 0;
+static const int depthReceiver = 2;
+static const int spacingReceiver = 2;
+static const int numberOfReceivers = 37;
+static const int numberOfTimeStep = 200;
+static const int sampligWavelet = 60;
+static const float cutFrequency = 50.0;
+static const int thicknessUp = 14;
+static const int thicknessDown = 16;
+static const int thicknessLeft = 18;
+static const int thicknessRight = 20;
+#endif
+'''
+
+_MAIN = r'''
+#include <stdio.h>
+#include <stdlib.h>
+#include "fixed_parameters.h"
+#define TIME_SLICES 20
+#include "rtm_dropin.h"
+int main(void)
+{
+    if (rtm_dropin_configure_from_fixed_parameters() != 0) return 2;
+    float *model = (float *)malloc(sizeof(float) * Nx * Nz);
+    float *ext = (float *)malloc(sizeof(float) * (Nx + thicknessLeft + thicknessRight) *
+                                 (Nz + thicknessUp + thicknessDown));
+    if (!model || !ext) return 3;
+    for (int i = 0; i < Nx * Nz; ++i) model[i] = (float)i;
+    extend_matrix(ext, model);        /* sizes from the configuration, no device work */
+    const int dz = Nz + thicknessUp + thicknessDown;
+    printf("%g %g %g\n", ext[0], ext[thicknessLeft * dz + thicknessUp],
+           ext[(thicknessLeft + Nx - 1) * dz + thicknessUp + Nz - 1]);
+    return 0;
+}
+'''
+
+
+def test_dropin_header_configures_from_fixed_parameters(engine, tmp_path):
+    """A program written against the reference's fixed_parameters.h includes rtm_dropin.h,
+    fills the library's configuration from those constants and calls a host entry point
+    (extend_matrix) with them: it compiles, links and runs without a GPU."""
+    import shutil
+    import subprocess
+    from rtmuq2d_gb300 import build as B
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    engine.dropin_lib()
+    (tmp_path / "fixed_parameters.h").write_text(_FIXED)
+    (tmp_path / "main.c").write_text(_MAIN)
+    libdir = os.path.dirname(B.DROPIN_LIB)
+    exe = tmp_path / "main"
+    subprocess.run([gcc, "-std=gnu99", "-I", str(tmp_path), "-I", os.path.join(ROOT, "include"),
+                    str(tmp_path / "main.c"), "-o", str(exe), "-L", libdir, "-lrtm_dropin", "-lrtmgpu",
+                    "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    # corner of the padding = model[0][0]; interior origin = model[0][0]; last interior cell
+    assert [float(v) for v in out] == [0.0, 0.0, float(37 * 29 - 1)]
