@@ -165,3 +165,25 @@ def test_large_field_encode_matches_reference_library(engine):
                                        f.shape[1], C.c_float(tol))
         assert n > 0
         assert C.string_at(ptr.value, n) == bytes(engine.zfp_encode(f, tol)), tol
+
+
+def test_random_and_truncated_streams_never_crash(engine):
+    """Random bytes and every truncation of a real stream decode to a status (OK or an
+    error), never past the buffer: the bit reader supplies zeros beyond the end and counts
+    them, and the decoder reports a stream it over-read."""
+    rng = np.random.default_rng(17)
+    f = (rng.standard_normal((37, 41)) * 0.3).astype(np.float32)
+    s = bytes(engine.zfp_encode(f, 1e-4))
+    for cut in range(0, len(s), max(1, len(s) // 97)):
+        try:
+            engine.zfp_decode(s[:cut], 37, 41, 1e-4)
+        except engine.RtmError:
+            pass
+    for n in (1, 7, 8, 9, 63, 64, 65, 500, 4096):
+        junk = rng.integers(0, 256, n, dtype=np.uint8).tobytes()
+        for tol in (1e-4, 0.0):
+            try:
+                out = engine.zfp_decode(junk, 37, 41, tol)
+                assert out.shape == (37, 41)
+            except engine.RtmError:
+                pass
