@@ -187,3 +187,26 @@ def test_random_and_truncated_streams_never_crash(engine):
                 assert out.shape == (37, 41)
             except engine.RtmError:
                 pass
+
+
+def test_codec_in_bounds_under_address_sanitizer(tmp_path):
+    """tests/zfp_fuzz.c against csrc/rtm_zfp.c built with AddressSanitizer and UBSan: every
+    truncation of a stream, random streams and the threaded encoder stay in bounds."""
+    import os
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "zfp_fuzz")
+    env = dict(os.environ, TMPDIR=str(tmp_path))
+    build = subprocess.run([gcc, "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                            "-fno-omit-frame-pointer", "-std=gnu99", "-I", os.path.join(root, "include"),
+                            os.path.join(root, "tests", "zfp_fuzz.c"),
+                            os.path.join(root, "rtmuq2d_gb300", "csrc", "rtm_zfp.c"), "-o", exe, "-lm",
+                            "-lpthread"], capture_output=True, text=True, env=env)
+    if build.returncode != 0:
+        pytest.skip("sanitizer build unavailable: " + build.stderr[-200:])
+    run = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=300)
+    assert run.returncode == 0, run.stderr[-2000:]
