@@ -166,3 +166,24 @@ def test_dropin_header_configures_from_fixed_parameters(engine, tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     # corner of the padding = model[0][0]; interior origin = model[0][0]; last interior cell
     assert [float(v) for v in out] == [0.0, 0.0, float(37 * 29 - 1)]
+
+
+def test_host_geometry_in_bounds_under_address_sanitizer(tmp_path):
+    """tests/host_fuzz.c against csrc/rtm_host.c built with AddressSanitizer and UBSan:
+    model padding and CPML profiles for 1 x 1 to 400 x 200 models and thicknesses 12-64."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "host_fuzz")
+    env = dict(os.environ, TMPDIR=str(tmp_path))
+    build = subprocess.run([gcc, "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+                            "-fno-omit-frame-pointer", "-std=gnu99", "-I", os.path.join(ROOT, "include"),
+                            os.path.join(ROOT, "tests", "host_fuzz.c"),
+                            os.path.join(ROOT, "rtmuq2d_gb300", "csrc", "rtm_host.c"), "-o", exe, "-lm"],
+                           capture_output=True, text=True, env=env)
+    if build.returncode != 0:
+        pytest.skip("sanitizer build unavailable: " + build.stderr[-200:])
+    run = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=300)
+    assert run.returncode == 0, run.stderr[-2000:]
