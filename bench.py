@@ -62,10 +62,15 @@ def parse():
     ap.add_argument("--serve-load-high", type=float, default=1.5,
                     help="second pass of the same trace at this load: a standing queue, the "
                          "server full (0: skip)")
+    ap.add_argument("--serve-capacity", type=float, default=150.0,
+                    help="with --only served: the batched capacity (Gcell-updates/s) the arrival "
+                         "rate is sized by")
     ap.add_argument("--steps-per-launch", type=int, default=16,
                     help="batched steps per CUDA-graph replay of the server")
     ap.add_argument("--precision-nt", type=int, default=7500,
                     help="reduced-precision storage study: time steps (0: skip)")
+    ap.add_argument("--only", default=None, choices=("batched", "served", "precision"),
+                    help="profiling only: run one form alone and print its JSON")
     return ap.parse_args()
 
 
@@ -93,10 +98,14 @@ def reduce_over_ranks(x, op, ws, device):
     return float(t.item())
 
 
-def workload(args, with_seis=True):
-    """Params and seeded host inputs of the benchmarked workload."""
+def workload(args, extend=None):
+    """Params and seeded host inputs of the benchmarked workload.  `extend` pads a model
+    into the CPML (default: the engine's extend_matrix; the reference arm passes the
+    oracle's, so that it never loads the engine library)."""
     from rtmuq2d_gb300 import workloads
-    import rtmuq2d_gb300 as eng
+    if extend is None:
+        import rtmuq2d_gb300 as eng
+        extend = eng.extend_matrix
     storage = 1 if args.storage == "ring" else 0
     if args.workload == "large":
         p = workloads.params_large(storage=storage)
@@ -105,8 +114,8 @@ def workload(args, with_seis=True):
         p = workloads.params_small(storage=storage)
         true, mig = workloads.models_small(p, seed=0)
     wav = workloads.wavelet_for(p)
-    ext_true = eng.extend_matrix(p, true)
-    ext = eng.extend_matrix(p, mig)
+    ext_true = extend(p, true)
+    ext = extend(p, mig)
     if args.nt:
         p = p.replace(nt=args.nt)
     if args.tile_x:
@@ -116,6 +125,16 @@ def workload(args, with_seis=True):
 
 def workload_name(p):
     return "rtm_single_shot_%dx%d_nt%d" % (p.nx, p.nz, p.nt)
+
+
+def bench_config(p, args, ws):
+    """The `config` of both arms' lines (the same keys and values: the same workload)."""
+    return {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
+            "receivers": p.rec_count, "storage": args.storage, "ring_precision": "fp32",
+            "seismogram": "modelled on the true model by the same scheme (trace recording)",
+            "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "GPU: L2 flushed between timed iterations (256 MB write); CPU: the snapshot "
+                  "store of the time axis (4.2 GB at 3500 x 800, nt 7500) streams through memory"}
 
 
 # the headline metric: Gcell-updates/s (value: the plain single-shot migration; the served
@@ -249,6 +268,84 @@ def cpu_sample(p, ext, wav, seis, target_s, dtype=np.float32):
             "kind": "port", "seconds": t,
             "sample": "forward+adjoint of the %dx%d padded grid for nt=%d of %d steps "
                       "(oracle/rtm_oracle.c, -O3 OpenMP)" % (p.dim_x, p.dim_z, nt, p.nt)}
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = float(np.linalg.norm(b))
+    return float(np.linalg.norm(a - b) / den) if den > 0 else None
+
+
+def cpu_full(p, ext_true, ext, wav, seis, img, slf):
+    """The CPU leg at full size: the oracle port (OpenMP over all host cores) models the
+    observed seismogram on the true model and migrates the same seismogram the GPU migrated.
+    Its migration time is the CPU baseline (the whole workload, not a sample); its outputs are
+    the parity reference of the GPU's recorded seismogram and image."""
+    from oracle.oracle import Oracle
+    orc = Oracle(fast=True)
+    q = p.as_dict()
+    t0 = time.perf_counter()
+    seis_ref = orc.model_seismogram(q, ext_true, wav)
+    t_model = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    img_ref, slf_ref = orc.migrate(q, ext, wav, seis)
+    t_mig = time.perf_counter() - t0
+    cpu = {"value": p.cell_updates / t_mig / 1e9, "unit": "Gcell-updates/s", "cores": orc.max_threads(),
+           "kind": "port",
+           "sample": "the whole workload: forward (snapshot storage) + adjoint of the %dx%d padded "
+                     "grid, nt=%d, in %.1f s (oracle/rtm_oracle.c, -O3, OpenMP)" % (p.dim_x, p.dim_z, p.nt, t_mig)}
+    parity = {"reference": "oracle port (-O3, OpenMP) on the same inputs",
+              "seis_rel_l2_vs_oracle": rel_l2(seis, seis_ref), "image_rel_l2_vs_oracle": rel_l2(img, img_ref),
+              "self_image_rel_l2_vs_oracle": rel_l2(slf, slf_ref), "oracle_model_seconds": t_model}
+    return cpu, parity
+
+
+def fp64_image(eng, p, ext, wav, seis):
+    """The image of an FP64 GPU run of the identical scheme (same storage, FP64 fields)."""
+    import torch
+    q = p.replace(compute=eng.COMPUTE_FP64, tile_x=0)
+    plan = eng.Plan(q)
+    plan.forward(torch.from_numpy(ext).cuda(), torch.from_numpy(wav).cuda())
+    plan.adjoint(torch.from_numpy(seis).cuda())
+    img = torch.empty((p.nx, p.nz), dtype=torch.float64, device="cuda")
+    plan.read_image(0, img, as_double=True)
+    plan.sync()
+    out = img.cpu().numpy()
+    plan.close()
+    return out
+
+
+def summary(line):
+    """The headline figures of every form in a few hundred bytes (the last key of the line)."""
+    def pick(d, *keys):
+        return {k: d.get(k) for k in keys} if d else None
+
+    def r3(x):
+        return round(x, 4) if isinstance(x, float) else x
+
+    out = {"plain": {"value": r3(line["value"]), "e2e": r3(line["e2e"]["value"]),
+                     "roofline_frac": r3(line["roofline"]["frac"])}}
+    b = line.get("batched")
+    if b:
+        out["batched"] = {k: r3(v) for k, v in pick(b, "value", "speedup_vs_plain", "members").items()}
+        for key, name in (("stencil_kernel_roofline", "k_mstep_frac"), ("forward_step_roofline", "fwd_step_frac")):
+            if b.get(key):
+                out["batched"][name] = r3(b[key]["frac"])
+        if b.get("autotuned"):
+            out["batched"]["tiles"] = b["autotuned"]
+    s = line.get("served")
+    if s:
+        out["served"] = {k: r3(v) for k, v in pick(s, "requests", "value", "p50_latency_s", "p99_latency_s",
+                                                   "hbm_occupancy_mean", "speedup_vs_plain_same_requests").items()}
+        if s.get("plain"):
+            out["served"]["plain_p50_s"] = r3(s["plain"].get("p50_latency_s"))
+            out["served"]["plain_p99_s"] = r3(s["plain"].get("p99_latency_s"))
+    par = line.get("parity")
+    if par:
+        out["parity"] = {k: (float("%.3g" % v) if isinstance(v, float) else v) for k, v in par.items()
+                         if k.endswith("rel_l2_vs_oracle") or k.endswith("fp64_engine")}
+    return out
 
 
 def run_batched(args, eng, rank=0, ws=1):
@@ -542,12 +639,17 @@ def run_precision(args, eng):
 
 
 def run_reference(args):
+    """The CPU implementation of the path on the host cores (the oracle port: the
+    reference's own build cannot travel to this machine).  Nothing here loads the engine
+    library: the padding and the observed seismogram come from the oracle too, the
+    seismogram modelled on the true model like the GPU arm's."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    p, ext_true, ext, wav = workload(args)
-    rng = np.random.default_rng(5)
-    seis = (rng.standard_normal((p.rec_count, p.nt)) * 1e-3).astype(np.float32)
+    from oracle.oracle import Oracle
+    orc = Oracle(fast=True)
+    p, ext_true, ext, wav = workload(args, extend=lambda q, m: orc.extend_matrix(q.as_dict(), m))
+    seis = orc.model_seismogram(p.as_dict(), ext_true, wav)
     target = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
         cpu_sample(p, ext, wav, seis, target / 4)
@@ -562,13 +664,25 @@ def run_reference(args):
             "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": cells_per_step / (v * 1e9) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
-                       "note": "each step times a bounded sample (shortened time axis) of the workload"},
+            "config": bench_config(p, args, ws),
+            "note": "each step times a bounded sample (the same grid, a shortened time axis) of the workload",
             "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": last["cores"],
                              "kind": last["kind"], "sample": last["sample"]},
             "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_only(args, eng):
+    """One form alone (profiling runs): its JSON, without the single-migration part."""
+    if args.only == "batched":
+        out = run_batched(args, eng)
+    elif args.only == "served":
+        out = run_served(args, eng, args.serve_capacity)
+    else:
+        out = run_precision(args, eng)
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -581,6 +695,8 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.only:
+        return run_only(args, eng)
     p, ext_true, ext, wav = workload(args)
     # observed data: forward modelling on the true model with trace recording (untimed)
     seis = eng.model_seismogram(p.replace(storage=0), ext_true, wav)
@@ -708,24 +824,25 @@ def run_gpu(args):
     precision = None
     if ws == 1 and args.precision_nt > 0:
         precision = run_precision(args, eng)
-    cpu = None
+    cpu, parity = None, None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_sample(p, ext, wav, seis, args.cpu_seconds)
-        cpu.pop("seconds", None)
+        # parity of this very run: the FP32 image and recorded seismogram against the oracle
+        # (full size), and the FP32 image against an FP64 GPU run of the identical scheme
+        cpu, parity = cpu_full(p, ext_true, ext, wav, seis, img_h, slf_h)
+        parity["image_rel_l2_vs_fp64_engine"] = rel_l2(img_h, fp64_image(eng, p, ext, wav, seis))
     line = {"metric": METRIC, "value": value,
             "unit": "Gcell-updates/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(p), "grid": [p.dim_x, p.dim_z], "nt": p.nt,
-                       "receivers": p.rec_count, "storage": args.storage, "ring_precision": "fp32",
-                       "parallelism": "replicas" if ws > 1 else "single", "autotuned": tuned,
-                       "l2": "flushed between timed iterations (256 MB write)"},
+            "config": bench_config(p, args, ws), "autotuned": tuned,
             "e2e": {"value": e2e_value, "unit": "Gcell-updates/s", "ms_per_step": e2e_total / args.steps,
                     "h2d_bytes_per_step": int(ext.nbytes + wav.nbytes + seis.nbytes),
                     "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
                     "entry_point": "rtm_migrate_shot", "image_agreement_rel_l2": agree},
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": sampler.summary(), "batched": batched, "served": served, "precision": precision}
+            "clocks": sampler.summary(), "precision": precision, "batched": batched, "served": served,
+            "parity": parity}
+    line["summary"] = summary(line)
     print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

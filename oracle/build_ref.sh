@@ -4,10 +4,11 @@
 # Test infrastructure: the result pins the oracle (rtm_oracle.c) and makes golden
 # fixtures.  The prebuilt ZFP objects/libraries shipped in the reference are not used.
 #
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]     (default /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   default: $RTM_REFERENCE_ROOT, else a "reference" directory beside the repository
 set -euo pipefail
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${RTM_REFERENCE_ROOT:-$HERE/../../reference}}
 OUT="$HERE/_ref"
 ZFP="$REF/ZFP_LIBRARY_0.5.5"
 if [ ! -d "$REF/SRC" ] || [ ! -d "$ZFP/src" ]; then

@@ -22,7 +22,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("RTM_REFERENCE_ROOT", "/root/reference")
+# the reference tree: RTM_REFERENCE_ROOT, else a "reference" directory beside the repository
+REFERENCE_ROOT = os.environ.get("RTM_REFERENCE_ROOT",
+                                os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 FIELDS_INT = ("nx", "nz", "th_left", "th_right", "th_up", "th_down")
 FIELDS_ALL = FIELDS_INT + ("dx", "dt", "nt", "n_wavelet", "shot_x", "shot_z", "rec_first",

@@ -10,7 +10,8 @@ on small seeded inputs:
   round trip through zfp2d_lossyCompression / zfp2d_lossyDecompression, and the whole
   driver rtm_routine on files (two shots, ZFP seismograms, stacked image and Laplacian).
 
-Needs the reference tree (default /root/reference, or RTM_REFERENCE_ROOT).  Run:
+Needs the reference tree (RTM_REFERENCE_ROOT, else a "reference" directory beside the
+repository).  Run:
     python tests/golden/make_golden.py
 """
 from __future__ import annotations

@@ -1,5 +1,9 @@
-"""The single-shot workload at full size (3400 x 700, CPML 50, nt 7500, 3400 receivers), where
-the oracle would take minutes, checked through properties that hold at any size:
+"""The single-shot workload at full size (3400 x 700, CPML 50, nt 7500, 3400 receivers).
+
+Against the oracle (its parity build, OpenMP over the host cores, about a minute): the
+recorded seismogram and the image and self image of both storages within relative L2 1e-4.
+
+And through properties that hold at any size:
 
 * the migration is linear in the seismogram: scaling it by a power of two scales the image by
   that factor and leaves the self image unchanged bit for bit; the image of a sum is the sum
@@ -41,6 +45,32 @@ def full(engine):
     ext = engine.extend_matrix(p, mig)
     seis = engine.model_seismogram(p, ext_true, wav)
     return p, ext_true, ext, wav, seis
+
+
+@pytest.fixture(scope="module")
+def full_oracle(oracle, full):
+    """The oracle's recorded seismogram, and its image and self image of that seismogram."""
+    p, ext_true, ext, wav, _ = full
+    seis_ref = oracle.model_seismogram(p.as_dict(), ext_true, wav)
+    img_ref, slf_ref = oracle.migrate(p.as_dict(), ext, wav, seis_ref)
+    return seis_ref, img_ref, slf_ref
+
+
+def test_full_size_seismogram_matches_oracle(full, full_oracle):
+    seis = full[4]
+    seis_ref = full_oracle[0]
+    assert np.abs(seis_ref).max() > 0
+    assert rel_l2(seis, seis_ref) <= 1e-4
+
+
+@pytest.mark.parametrize("storage", (1, 0))
+def test_full_size_image_matches_oracle(engine, full, full_oracle, storage):
+    p, _, ext, wav, _ = full
+    seis_ref, img_ref, slf_ref = full_oracle
+    img, slf = engine.migrate_shot(p.replace(storage=storage), ext, wav, seis_ref)
+    assert np.abs(img_ref).max() > 0
+    assert rel_l2(img, img_ref) <= 1e-4
+    assert rel_l2(slf, slf_ref) <= 1e-4
 
 
 def test_full_size_modeling_is_linear_in_the_wavelet(engine, full):

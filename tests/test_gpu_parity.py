@@ -169,6 +169,56 @@ def test_small_workload_against_oracle(engine, oracle):
         assert rel_l2(slf, ref_slf) <= 1e-4, storage
 
 
+@pytest.fixture(scope="module")
+def small_workload(engine, oracle):
+    """The 400 x 200, nt 2000 workload (CPML 40, 400 receivers) with its observed seismogram
+    modelled by the oracle on the true model."""
+    from rtmuq2d_gb300 import workloads
+    p = workloads.params_small()
+    true, mig = workloads.models_small(p, seed=0)
+    wav = workloads.wavelet_for(p)
+    ext_true = engine.extend_matrix(p, true)
+    ext = engine.extend_matrix(p, mig)
+    seis = oracle.model_seismogram(p.as_dict(), ext_true, wav)
+    return p, ext, wav, seis
+
+
+def test_small_workload_through_zfp_matches_oracle(engine, oracle, small_workload):
+    """The 400 x 200 workload as its configuration states it: the observed seismogram a ZFP
+    fixed-accuracy stream at tolerance 1e-4 (written by the codec that is byte-identical to
+    the reference's library), decoded on the host by the server and by the file-level path;
+    the served and the plain images against the oracle's migration of the decoded data."""
+    p, ext, wav, seis = small_workload
+    tol = 1e-4
+    stream = engine.zfp_encode(seis, tol)
+    dec = engine.zfp_decode(stream, p.rec_count, p.nt, tol).reshape(p.rec_count, p.nt)
+    assert np.max(np.abs(dec - seis)) <= tol and len(stream) < seis.nbytes
+    ref_img, ref_slf = oracle.migrate(p.as_dict(), ext, wav, dec)
+    srv = engine.Server(0, max_members=4)
+    rid = srv.submit_zfp(p, ext, wav, stream, tol)
+    img, slf, _ = srv.wait(rid)
+    srv.close()
+    assert rel_l2(img, ref_img) <= 1e-4 and rel_l2(slf, ref_slf) <= 1e-4
+    img, slf = engine.migrate_shot(p, ext, wav, dec)
+    assert rel_l2(img, ref_img) <= 1e-4 and rel_l2(slf, ref_slf) <= 1e-4
+
+
+@pytest.mark.parametrize("storage", (0, 1))
+@pytest.mark.parametrize("precision", (1, 2))
+def test_16bit_storage_within_1e3_of_fp64_oracle(engine, oracle, small_workload, storage, precision):
+    """BF16 / FP16 source-wavefield storage (per-step, per-tile max-abs scales; stencil and
+    CPML in FP32, image in FP64) on the 400 x 200, nt 2000 workload: the image within relative
+    L2 1e-3 of the FP64 oracle's image of the identical scheme."""
+    p, ext, wav, seis = small_workload
+    ref_img, ref_slf = oracle.migrate(p.as_dict(), ext, wav, seis, dtype=np.float64)
+    q = p.replace(storage=storage, precision=precision)
+    img, slf = engine.migrate_shot(q, ext, wav, seis)
+    fp32, _ = engine.migrate_shot(q.replace(precision=0), ext, wav, seis)
+    assert not np.array_equal(img, fp32)     # the 16-bit path really ran
+    assert rel_l2(img, ref_img) <= 1e-3
+    assert rel_l2(slf, ref_slf) <= 1e-3
+
+
 @pytest.mark.parametrize("storage", (0, 1))
 @pytest.mark.parametrize("precision,tol", ((1, 5e-2), (2, 5e-3)))
 def test_16bit_storage_close_to_fp32(engine, storage, precision, tol):
