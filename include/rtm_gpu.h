@@ -111,6 +111,33 @@ int rtm_adjoint_modeling(const rtm_params *p, int sim_id, const int *shot,
                          const float *velocity, const float *wavelet,
                          const float *seismogram, float *image, float *self_image);
 
+/* ---- shot stack on the device ---------------------------------------------------------------
+ * The stacking of SRC/rtm_iso2d.c:108-165 without its host round trips: each shot's image and
+ * self image are added to float32 stacks (nx x nz) in device memory where the adjoint pass
+ * leaves them, in shot order and in the reference's arithmetic (the shot's image rounded to
+ * float, then a float sum: rtm_iso2d.c:121-126), and the final stack and its Laplacian
+ * (laplacian_filter2D, math_functions.c:9-27) are computed on the device and come back to the
+ * host in one copy.  The reference sums per-shot temporary files on the host instead. */
+typedef struct rtm_stack rtm_stack;
+int rtm_stack_create(const rtm_params *p, rtm_stack **stack);   /* zeroed stacks of p's nx x nz */
+int rtm_stack_destroy(rtm_stack *stack);
+/* Sets both stacks from host arrays (NULL: zeros), e.g. when resuming from a checkpoint. */
+int rtm_stack_load(rtm_stack *stack, const float *image_stack, const float *self_stack);
+/* rtm_adjoint_modeling with the shot's image and self image added to the device stacks
+ * instead of to host arrays; consumes the sim_id state of rtm_forward_modeling. */
+int rtm_adjoint_modeling_stacked(const rtm_params *p, int sim_id, const int *shot,
+                                 const float *seismogram, rtm_stack *stack);
+/* The running image and self-image stacks to the host (one copy), e.g. for a checkpoint. */
+int rtm_stack_read_raw(rtm_stack *stack, float *image_stack, float *self_stack);
+/* The stacked image -- the image stack, or with normalize_by_self the image stack divided by
+ * the self-image stack (the branch rtm_iso2d.c:150-156 leaves commented out), where a pixel
+ * whose self-image stack is 0 (no source energy reached it) is 0 rather than the reference's
+ * 0/0 or x/0 -- and its Laplacian, computed on the device, to the host in one copy.
+ * RTM_ERR_TIMEOUT if a stacked shot's kernels reported a timed-out wait. */
+int rtm_stack_finish(rtm_stack *stack, int normalize_by_self, float *stacked, float *laplacian);
+/* Device-to-host copies (and bytes) the stack has made since its creation. */
+int rtm_stack_transfers(const rtm_stack *stack, long long *d2h_copies, long long *d2h_bytes);
+
 /* Forward + adjoint of one shot in one call (rtm_iso2d.c:85-93 without the decode). */
 int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wavelet,
                      const float *seismogram, float *image, float *self_image);
@@ -323,6 +350,10 @@ typedef struct rtm_survey {
  * stack when normalize_by_self is set); both output files are written.  RTM_ERR_IO when an
  * input cannot be read or an output written (the reference exits instead). */
 int rtm_routine_run(const rtm_params *p, const rtm_survey *survey, int simulation_id);
+/* Device-to-host copies (and bytes) the last rtm_routine_run on the calling thread made of its
+ * stacks: 1 without a checkpoint file (the final stack with its Laplacian), plus one per shot
+ * with one.  RTM_ERR_STATE (and -1s) if no run has finished on this thread. */
+int rtm_routine_last_transfers(long long *d2h_copies, long long *d2h_bytes);
 /* rtm_routine over several simulations on one GPU (replaces the MPI fan-out of
  * mpi_rtm_iso2d.c:39-51): every (simulation, shot) migration is a request of one batched
  * server (rtm_server_*; budget and member slots as rtm_server_create takes them, 0 = default),

@@ -183,6 +183,14 @@ def _declare(L):
                                              C.POINTER(C.c_size_t)]),
         "rtm_routine_run": (C.c_int, [P, C.POINTER(RtmSurvey), C.c_int]),
         "rtm_routine_batch": (C.c_int, [P, C.POINTER(RtmSurvey), ip, C.c_int, C.c_longlong, C.c_int]),
+        "rtm_routine_last_transfers": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "rtm_stack_create": (C.c_int, [P, C.POINTER(vp)]),
+        "rtm_stack_destroy": (C.c_int, [vp]),
+        "rtm_stack_load": (C.c_int, [vp, fp, fp]),
+        "rtm_adjoint_modeling_stacked": (C.c_int, [P, C.c_int, ip, fp, vp]),
+        "rtm_stack_read_raw": (C.c_int, [vp, fp, fp]),
+        "rtm_stack_finish": (C.c_int, [vp, C.c_int, fp, fp]),
+        "rtm_stack_transfers": (C.c_int, [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "rtm_plan_profile": (C.c_int, [vp, C.c_int]),
         "rtm_plan_profile_read": (C.c_int, [vp, C.POINTER(C.c_double), ip, C.POINTER(C.c_double), ip]),
     }
@@ -207,7 +215,9 @@ def exported_symbols():
             "rtm_server_step",
             "rtm_server_poll", "rtm_server_wait", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
             "rtm_zfp_decode_float2d", "rtm_zfp_decode_file", "rtm_zfp_encode_bound",
-            "rtm_zfp_encode_float2d", "rtm_routine_run", "rtm_routine_batch"]
+            "rtm_zfp_encode_float2d", "rtm_routine_run", "rtm_routine_batch", "rtm_routine_last_transfers",
+            "rtm_stack_create", "rtm_stack_destroy", "rtm_stack_load", "rtm_adjoint_modeling_stacked",
+            "rtm_stack_read_raw", "rtm_stack_finish", "rtm_stack_transfers"]
 
 
 def status_string(st: int) -> str:
@@ -362,6 +372,68 @@ def routine_batch(p: RtmParams, survey: RtmSurvey, simulation_ids, hbm_budget_by
     ids = (C.c_int * len(simulation_ids))(*[int(i) for i in simulation_ids])
     _check(lib().rtm_routine_batch(C.byref(p), C.byref(survey), ids, len(simulation_ids),
                                    int(hbm_budget_bytes), int(max_members)))
+
+
+def routine_last_transfers():
+    """(device-to-host copies, bytes) of the last routine_run on this thread."""
+    c, b = C.c_longlong(), C.c_longlong()
+    _check(lib().rtm_routine_last_transfers(C.byref(c), C.byref(b)))
+    return c.value, b.value
+
+
+class Stack:
+    """Shot stack in device memory (include/rtm_gpu.h, rtm_stack_*): shots' images added where
+    the adjoint pass leaves them, the final stack and its Laplacian back in one copy."""
+
+    def __init__(self, p: RtmParams):
+        self.params = p.replace()
+        h = C.c_void_p()
+        _check(lib().rtm_stack_create(C.byref(self.params), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().rtm_stack_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, image_stack=None, self_stack=None):
+        a = _f32(image_stack) if image_stack is not None else None
+        b = _f32(self_stack) if self_stack is not None else None
+        _check(lib().rtm_stack_load(self.handle, _fp(a) if a is not None else None,
+                                    _fp(b) if b is not None else None))
+
+    def adjoint(self, p: RtmParams, sim_id: int, shot, seismogram) -> None:
+        """rtm_adjoint_modeling of sim_id's forward state, added to this stack."""
+        sh = (C.c_int * 2)(*shot)
+        s = _f32(seismogram) if seismogram is not None else None
+        _check(lib().rtm_adjoint_modeling_stacked(C.byref(p), sim_id, sh, _fp(s) if s is not None else None,
+                                                  self.handle))
+
+    def read_raw(self):
+        p = self.params
+        img = np.empty((p.nx, p.nz), np.float32)
+        slf = np.empty((p.nx, p.nz), np.float32)
+        _check(lib().rtm_stack_read_raw(self.handle, _fp(img), _fp(slf)))
+        return img, slf
+
+    def finish(self, normalize_by_self: bool = False):
+        """(stacked image, its Laplacian), nx x nz each."""
+        p = self.params
+        out = np.empty((p.nx, p.nz), np.float32)
+        lap = np.empty((p.nx, p.nz), np.float32)
+        _check(lib().rtm_stack_finish(self.handle, int(bool(normalize_by_self)), _fp(out), _fp(lap)))
+        return out, lap
+
+    def transfers(self):
+        c, b = C.c_longlong(), C.c_longlong()
+        _check(lib().rtm_stack_transfers(self.handle, C.byref(c), C.byref(b)))
+        return c.value, b.value
 
 
 def dropin_lib():

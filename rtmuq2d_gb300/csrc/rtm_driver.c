@@ -4,14 +4,15 @@
  *
  * Same inputs, outputs and arithmetic of the stack as the reference: velocity and wavelet
  * read raw (pi_file.c:11-32), edge-replicated into the CPML (extend_matrix), per shot a
- * forward propagation, the shot's ZFP seismogram decoded, an adjoint propagation into a
- * zeroed image and self image; images and self images summed over shots in float32 in shot
- * order (rtm_iso2d.c:115-129), optionally the image stack divided by the self-image stack
- * (the whole-survey branch the reference leaves commented out, rtm_iso2d.c:150-156), the
+ * forward propagation, the shot's ZFP seismogram decoded, an adjoint propagation; images and
+ * self images summed over shots in float32 in shot order (rtm_iso2d.c:115-129), optionally
+ * the image stack divided by the self-image stack (the whole-survey branch the reference
+ * leaves commented out, rtm_iso2d.c:150-156; a pixel with a zero self-image stack is 0), the
  * stack written, its Laplacian (laplacian_filter2D) written.
- * Differences: the per-shot images stay in host memory instead of TEMPORARY_FILES
- * round trips (rtm_iso2d.c:95-103, 108-140), the seismograms are decoded ahead on host
- * threads while the GPU migrates earlier shots, errors are returned
+ * Differences: the stacks stay in device memory (rtm_stack: each shot's image is added where
+ * the adjoint pass leaves it, and only the final stack and its Laplacian come back, in one
+ * copy) instead of TEMPORARY_FILES round trips (rtm_iso2d.c:95-103, 108-140), the seismograms
+ * are decoded ahead on host threads while the GPU migrates earlier shots, errors are returned
  * (RTM_ERR_IO) where the reference exits, and, with a checkpoint file, the stacks are saved
  * after each shot so that a run stopped by a failure resumes after its last finished shot.
  */
@@ -42,13 +43,45 @@ static int write_raw(const char *path, const float *src, size_t n)
     return (put == n && closed == 0) ? RTM_OK : RTM_ERR_IO;
 }
 
-/* Checkpoint of a simulation's shot stack: "RTMCKPT1", int32 simulation id, nx, nz, n_shots,
- * shots done, then the image stack and the self-image stack (float32, nx * nz each).  Written
- * to `path`.tmp and renamed over `path`, so a reader sees a whole file or the previous one. */
-static const char kCkptMagic[8] = {'R', 'T', 'M', 'C', 'K', 'P', 'T', '1'};
+/* Checkpoint of a simulation's shot stack: "RTMCKPT2", int32 simulation id, nx, nz, n_shots,
+ * shots done, a 64-bit key of the run, then the image stack and the self-image stack (float32,
+ * nx * nz each).  Written to `path`.tmp and renamed over `path`, so a reader sees a whole file
+ * or the previous one.  The key (FNV-1a over the migration parameters, the survey's shot
+ * geometry, ZFP tolerance and normalisation, and the input file names of this simulation)
+ * keeps a checkpoint of another survey of the same shape from being resumed. */
+static const char kCkptMagic[8] = {'R', 'T', 'M', 'C', 'K', 'P', 'T', '2'};
+
+static unsigned long long fnv1a(unsigned long long h, const void *data, size_t n)
+{
+    const unsigned char *b = (const unsigned char *)data;
+    for (size_t i = 0; i < n; ++i) {
+        h ^= b[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+static unsigned long long run_key(const rtm_params *p, const rtm_survey *s, int sim)
+{
+    rtm_params q = *p;
+    q.shot_x = q.shot_z = 0;             /* per shot; the survey's geometry is keyed below */
+    unsigned long long h = 14695981039346656037ull;
+    h = fnv1a(h, &q, sizeof q);
+    const int geo[5] = {s->first_shot, s->shot_depth, s->shot_spacing, s->n_shots, s->normalize_by_self};
+    h = fnv1a(h, geo, sizeof geo);
+    h = fnv1a(h, &s->zfp_tolerance, sizeof s->zfp_tolerance);
+    char path[RTM_PATH_LEN];
+    const char *pats[3] = {s->velocity_file, s->wavelet_file, s->seismogram_file};
+    for (int k = 0; k < 3; ++k) {
+        const int n = snprintf(path, sizeof path, pats[k], sim);
+        if (n > 0) h = fnv1a(h, path, (size_t)(n < RTM_PATH_LEN ? n : RTM_PATH_LEN - 1));
+        h = fnv1a(h, "|", 1);
+    }
+    return h;
+}
 
 static int ckpt_write(const char *path, int sim, int nx, int nz, int n_shots, int done,
-                      const float *stack, const float *sstack, size_t n)
+                      unsigned long long key, const float *stack, const float *sstack, size_t n)
 {
     char tmp[RTM_PATH_LEN + 8];
     const int len = snprintf(tmp, sizeof tmp, "%s.tmp", path);
@@ -57,6 +90,7 @@ static int ckpt_write(const char *path, int sim, int nx, int nz, int n_shots, in
     if (!f) return RTM_ERR_IO;
     const int hdr[5] = {sim, nx, nz, n_shots, done};
     int ok = fwrite(kCkptMagic, 1, 8, f) == 8 && fwrite(hdr, sizeof(int), 5, f) == 5 &&
+             fwrite(&key, sizeof key, 1, f) == 1 &&
              fwrite(stack, sizeof(float), n, f) == n && fwrite(sstack, sizeof(float), n, f) == n;
     ok = (fclose(f) == 0) && ok;
     if (!ok || rename(tmp, path) != 0) {
@@ -67,18 +101,19 @@ static int ckpt_write(const char *path, int sim, int nx, int nz, int n_shots, in
 }
 
 /* Shots already stacked by a matching checkpoint (0: none, or one of another run). */
-static int ckpt_read(const char *path, int sim, int nx, int nz, int n_shots, float *stack,
-                     float *sstack, size_t n)
+static int ckpt_read(const char *path, int sim, int nx, int nz, int n_shots, unsigned long long key,
+                     float *stack, float *sstack, size_t n)
 {
     FILE *f = fopen(path, "rb");
     if (!f) return 0;
     char magic[8];
     int hdr[5];
+    unsigned long long k = 0;
     int done = 0;
     if (fread(magic, 1, 8, f) == 8 && memcmp(magic, kCkptMagic, 8) == 0 &&
         fread(hdr, sizeof(int), 5, f) == 5 && hdr[0] == sim && hdr[1] == nx && hdr[2] == nz &&
-        hdr[3] == n_shots && hdr[4] > 0 && hdr[4] <= n_shots &&
-        fread(stack, sizeof(float), n, f) == n && fread(sstack, sizeof(float), n, f) == n)
+        hdr[3] == n_shots && hdr[4] > 0 && hdr[4] <= n_shots && fread(&k, sizeof k, 1, f) == 1 &&
+        k == key && fread(stack, sizeof(float), n, f) == n && fread(sstack, sizeof(float), n, f) == n)
         done = hdr[4];
     fclose(f);
     if (!done) {                          /* not ours: start from zero stacks */
@@ -89,10 +124,22 @@ static int ckpt_read(const char *path, int sim, int nx, int nz, int n_shots, flo
 }
 
 /* rtm_iso2d.c:148-156: the whole-survey branch divides the stack by the self-image stack
- * (commented out in the reference, which keeps the plain stack). */
+ * (commented out in the reference, which keeps the plain stack).  A pixel whose self-image
+ * stack is 0 -- no source energy reached it -- is set to 0, where the reference's division
+ * would write 0/0 (NaN) or x/0 (inf); rtm_stack_finish applies the same rule on the device. */
 static void normalize_stack(float *stack, const float *self_stack, size_t n)
 {
-    for (size_t i = 0; i < n; ++i) stack[i] = stack[i] / self_stack[i];
+    for (size_t i = 0; i < n; ++i) stack[i] = self_stack[i] != 0.0f ? stack[i] / self_stack[i] : 0.0f;
+}
+
+/* Device-to-host copies of the last rtm_routine_run on this thread (see rtm_routine_last_transfers). */
+static __thread long long t_last_d2h_copies = -1, t_last_d2h_bytes = -1;
+
+int rtm_routine_last_transfers(long long *d2h_copies, long long *d2h_bytes)
+{
+    if (d2h_copies) *d2h_copies = t_last_d2h_copies;
+    if (d2h_bytes) *d2h_bytes = t_last_d2h_bytes;
+    return t_last_d2h_copies < 0 ? RTM_ERR_STATE : RTM_OK;
 }
 
 static int format_path(char *out, const char *pattern, int id)
@@ -183,13 +230,13 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     float *ext = (float *)calloc(next, sizeof(float));
     float *wav = (float *)calloc(nwav, sizeof(float));
     float *seis = NULL;
-    float *img = (float *)calloc(nimg, sizeof(float));
-    float *slf = (float *)calloc(nimg, sizeof(float));
     float *stack = (float *)calloc(nimg, sizeof(float));
     float *sstack = (float *)calloc(nimg, sizeof(float));
     float *lap = (float *)calloc(nimg, sizeof(float));
     char path[RTM_PATH_LEN], ckpt[RTM_PATH_LEN];
     int first_shot = 1;
+    rtm_stack *dstack = NULL;
+    unsigned long long ckey = 0;
     decode_ahead dec;
     pthread_t workers[4];
     int nworkers = 0;
@@ -198,13 +245,17 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
     pthread_cond_init(&dec.cv, NULL);
     dec.buf = (float **)calloc((size_t)s->n_shots + 1, sizeof(float *));
     dec.st = (int *)calloc((size_t)s->n_shots + 1, sizeof(int));
-    if (!model || !ext || !wav || !img || !slf || !stack || !sstack || !lap || !dec.buf || !dec.st) {
+    t_last_d2h_copies = t_last_d2h_bytes = -1;
+    if (!model || !ext || !wav || !stack || !sstack || !lap || !dec.buf || !dec.st) {
         st = RTM_ERR_NOMEM;
         goto done;
     }
+    if ((st = rtm_stack_create(&p, &dstack)) != RTM_OK) goto done;
     if (s->checkpoint_file) {             /* resume after the shots a checkpoint holds */
         if ((st = format_path(ckpt, s->checkpoint_file, simulation_id)) != RTM_OK) goto done;
-        first_shot = 1 + ckpt_read(ckpt, simulation_id, p.nx, p.nz, s->n_shots, stack, sstack, nimg);
+        ckey = run_key(&p, s, simulation_id);
+        first_shot = 1 + ckpt_read(ckpt, simulation_id, p.nx, p.nz, s->n_shots, ckey, stack, sstack, nimg);
+        if (first_shot > 1 && (st = rtm_stack_load(dstack, stack, sstack)) != RTM_OK) goto done;
     }
     /* the shots' seismograms decode ahead on up to four host threads */
     dec.p = &p;
@@ -237,26 +288,25 @@ int rtm_routine_run(const rtm_params *params, const rtm_survey *s, int simulatio
         /* decoded meanwhile (or before) by the decode-ahead threads */
         free(seis);
         if (!(seis = decode_take(&dec, shot_id, &st))) goto done;
-        memset(img, 0, nimg * sizeof(float));
-        memset(slf, 0, nimg * sizeof(float));
-        if ((st = rtm_adjoint_modeling(&p, simulation_id, shot, ext, wav, seis, img, slf)) != RTM_OK) goto done;
-        /* rtm_iso2d.c:121-126: float sums in shot order */
-        for (size_t i = 0; i < nimg; ++i) {
-            stack[i] = stack[i] + img[i];
-            sstack[i] = sstack[i] + slf[i];
+        /* rtm_iso2d.c:121-126: float sums in shot order, on the device */
+        if ((st = rtm_adjoint_modeling_stacked(&p, simulation_id, shot, seis, dstack)) != RTM_OK) goto done;
+        if (s->checkpoint_file) {
+            if ((st = rtm_stack_read_raw(dstack, stack, sstack)) != RTM_OK) goto done;
+            if ((st = ckpt_write(ckpt, simulation_id, p.nx, p.nz, s->n_shots, shot_id, ckey, stack, sstack,
+                                 nimg)) != RTM_OK)
+                goto done;
         }
-        if (s->checkpoint_file &&
-            (st = ckpt_write(ckpt, simulation_id, p.nx, p.nz, s->n_shots, shot_id, stack, sstack, nimg)) != RTM_OK)
-            goto done;
     }
-    if (s->normalize_by_self) normalize_stack(stack, sstack, nimg);
+    /* the stack (normalised if asked) and its Laplacian, computed on the device: one copy back */
+    if ((st = rtm_stack_finish(dstack, s->normalize_by_self, stack, lap)) != RTM_OK) goto done;
+    rtm_stack_transfers(dstack, &t_last_d2h_copies, &t_last_d2h_bytes);
     if ((st = format_path(path, s->stacked_file, simulation_id)) != RTM_OK) goto done;
     if ((st = write_raw(path, stack, nimg)) != RTM_OK) goto done;
-    if ((st = rtm_laplacian_filter2D(&p, lap, stack)) != RTM_OK) goto done;
     if ((st = format_path(path, s->laplacian_file, simulation_id)) != RTM_OK) goto done;
     st = write_raw(path, lap, nimg);
     if (st == RTM_OK && s->checkpoint_file) remove(ckpt);   /* the outputs hold the result */
 done:
+    if (dstack) rtm_stack_destroy(dstack);
     pthread_mutex_lock(&dec.mu);
     dec.stop = 1;
     pthread_cond_broadcast(&dec.cv);
@@ -268,7 +318,7 @@ done:
     pthread_cond_destroy(&dec.cv);
     pthread_mutex_destroy(&dec.mu);
     free(model); free(ext); free(wav); free(seis);
-    free(img); free(slf); free(stack); free(sstack); free(lap);
+    free(stack); free(sstack); free(lap);
     return st;
 }
 

@@ -1243,6 +1243,191 @@ int rtm_model_seismogram(const rtm_params *p, const float *velocity, const float
     return st;
 }
 
+}  // extern "C"
+
+// ---- shot stack on the device ----------------------------------------------------------
+// One allocation: acc = [image stack | self-image stack] (float32, nx x nz each, [x][z]),
+// out = [stacked image | its Laplacian], then the status word, so that the final result and
+// the status come back in one copy.
+struct rtm_stack {
+    rtm_params p;
+    Geom g;
+    size_t n = 0;
+    unsigned char *base = nullptr;
+    float *acc_img = nullptr, *acc_slf = nullptr, *out = nullptr;
+    unsigned *status = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t last_add = nullptr;    // the latest shot's accumulation (shot order)
+    bool added = false;
+    float *h_pinned = nullptr;         // 2n floats + the status word
+    long long d2h_copies = 0, d2h_bytes = 0;
+};
+
+namespace rtm {
+
+static void stack_free(rtm_stack *S)
+{
+    if (!S) return;
+    if (S->stream) cudaStreamSynchronize(S->stream);
+    if (S->last_add) cudaEventDestroy(S->last_add);
+    if (S->base) cudaFree(S->base);
+    if (S->h_pinned) cudaFreeHost(S->h_pinned);
+    if (S->stream) cudaStreamDestroy(S->stream);
+    delete S;
+}
+
+// Makes the stack's stream wait for the latest accumulation.
+static int stack_order(rtm_stack *S, cudaStream_t s)
+{
+    if (S->added) RTM_CUDA(cudaStreamWaitEvent(s, S->last_add, 0));
+    return RTM_OK;
+}
+
+}  // namespace rtm
+
+extern "C" {
+
+int rtm_stack_create(const rtm_params *p, rtm_stack **out)
+{
+    if (!p || !out) return fail(RTM_ERR_INVALID, "null argument");
+    *out = nullptr;
+    RTM_TRY(check_params(*p));
+    std::unique_ptr<rtm_stack> S(new rtm_stack());
+    S->p = *p;
+    S->g = make_geom(*p);
+    S->n = (size_t)p->nx * p->nz;
+    const size_t bytes = 4 * S->n * sizeof(float) + 256;
+    cudaError_t e = cudaMalloc(&S->base, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        S->base = nullptr;
+        return fail(RTM_ERR_NOMEM, "cudaMalloc(%zu bytes) for the shot stack: %s", bytes, cudaGetErrorString(e));
+    }
+    float *f = reinterpret_cast<float *>(S->base);
+    S->acc_img = f;
+    S->acc_slf = f + S->n;
+    S->out = f + 2 * S->n;
+    S->status = reinterpret_cast<unsigned *>(f + 4 * S->n);
+    rtm_stack *raw = S.release();
+    auto bail = [&](int st) { stack_free(raw); return st; };
+    if (cudaStreamCreateWithFlags(&raw->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&raw->last_add, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost(&raw->h_pinned, 2 * raw->n * sizeof(float) + sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(RTM_ERR_CUDA, "shot stack: stream, event or pinned buffer"));
+    }
+    if (cudaMemsetAsync(raw->base, 0, bytes, raw->stream) != cudaSuccess ||
+        cudaStreamSynchronize(raw->stream) != cudaSuccess)
+        return bail(fail(RTM_ERR_CUDA, "shot stack: clear"));
+    *out = raw;
+    return RTM_OK;
+}
+
+int rtm_stack_destroy(rtm_stack *stack)
+{
+    stack_free(stack);
+    return RTM_OK;
+}
+
+int rtm_stack_load(rtm_stack *S, const float *image_stack, const float *self_stack)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null stack");
+    RTM_TRY(stack_order(S, S->stream));
+    const size_t b = S->n * sizeof(float);
+    RTM_CUDA(cudaStreamSynchronize(S->stream));    // the pinned buffer is free
+    if (image_stack) memcpy(S->h_pinned, image_stack, b);
+    else memset(S->h_pinned, 0, b);
+    if (self_stack) memcpy(S->h_pinned + S->n, self_stack, b);
+    else memset(S->h_pinned + S->n, 0, b);
+    RTM_CUDA(cudaMemcpyAsync(S->acc_img, S->h_pinned, 2 * b, cudaMemcpyHostToDevice, S->stream));
+    RTM_CUDA(cudaEventRecord(S->last_add, S->stream));
+    S->added = true;
+    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    return RTM_OK;
+}
+
+int rtm_adjoint_modeling_stacked(const rtm_params *p, int sim_id, const int *shot, const float *seismogram,
+                                 rtm_stack *S)
+{
+    if (!p || !S || (!seismogram && p->rec_count > 0)) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->nx != S->p.nx || p->nz != S->p.nz) return fail(RTM_ERR_INVALID, "stack of another image size");
+    rtm_plan *P = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_sim.find(sim_id);
+        if (it == g_sim.end()) return fail(RTM_ERR_STATE, "no forward state for simulation %d", sim_id);
+        P = it->second;
+        g_sim.erase(it);
+    }
+    if (!same_params(P->p, with_shot(p, shot))) {
+        release_plan(P);
+        return fail(RTM_ERR_INVALID, "parameters differ from the forward pass of simulation %d", sim_id);
+    }
+    auto run = [&]() -> int {
+        const Geom &g = P->g;
+        float *stage = P->at<float>(P->L.staging);
+        if (g.nrec > 0) RTM_TRY(upload_host(P, stage, seismogram, sizeof(float) * (size_t)g.nrec * g.nt));
+        RTM_TRY(dispatch_adjoint(P, stage));
+        if (!P->image_valid) return fail(RTM_ERR_STATE, "no image after the adjoint pass");
+        RTM_TRY(stack_order(S, P->stream));           // the shots' sums in shot order
+        RTM_CUDA(launch_stack_add(g, P->at<double>(P->L.img), P->at<double>(P->L.slf), S->acc_img, S->acc_slf,
+                                  P->at<unsigned>(P->L.status), S->status, P->stream));
+        P->launches++;
+        RTM_CUDA(cudaEventRecord(S->last_add, P->stream));
+        S->added = true;
+        return RTM_OK;
+    };
+    const int st = run();
+    release_plan(P);
+    return st;
+}
+
+int rtm_stack_read_raw(rtm_stack *S, float *image_stack, float *self_stack)
+{
+    if (!S || !image_stack || !self_stack) return fail(RTM_ERR_INVALID, "null argument");
+    RTM_TRY(stack_order(S, S->stream));
+    const size_t b = 2 * S->n * sizeof(float);
+    RTM_CUDA(cudaMemcpyAsync(S->h_pinned, S->acc_img, b, cudaMemcpyDeviceToHost, S->stream));
+    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    S->d2h_copies++;
+    S->d2h_bytes += (long long)b;
+    memcpy(image_stack, S->h_pinned, S->n * sizeof(float));
+    memcpy(self_stack, S->h_pinned + S->n, S->n * sizeof(float));
+    return RTM_OK;
+}
+
+int rtm_stack_finish(rtm_stack *S, int normalize_by_self, float *stacked, float *laplacian)
+{
+    if (!S || !stacked || !laplacian) return fail(RTM_ERR_INVALID, "null argument");
+    const int nx = S->p.nx, nz = S->p.nz;
+    const size_t n = S->n;
+    float *out = S->out, *lap = S->out + n;
+    RTM_TRY(stack_order(S, S->stream));
+    RTM_CUDA(launch_stack_finish((int)n, S->acc_img, S->acc_slf, normalize_by_self, out, S->stream));
+    RTM_CUDA(cudaMemsetAsync(lap, 0, n * sizeof(float), S->stream));
+    RTM_CUDA(launch_laplacian(nx, nz, out, lap, S->stream));
+    // stacked image, Laplacian and status word: one copy
+    const size_t b = 2 * n * sizeof(float) + sizeof(unsigned);
+    RTM_CUDA(cudaMemcpyAsync(S->h_pinned, out, b, cudaMemcpyDeviceToHost, S->stream));
+    RTM_CUDA(cudaStreamSynchronize(S->stream));
+    S->d2h_copies++;
+    S->d2h_bytes += (long long)b;
+    unsigned st;
+    memcpy(&st, S->h_pinned + 2 * n, sizeof st);
+    if (st & ST_TMA_TIMEOUT) return fail(RTM_ERR_TIMEOUT, "a tile load of a stacked shot did not complete within its time limit");
+    memcpy(stacked, S->h_pinned, n * sizeof(float));
+    memcpy(laplacian, S->h_pinned + n, n * sizeof(float));
+    return RTM_OK;
+}
+
+int rtm_stack_transfers(const rtm_stack *S, long long *d2h_copies, long long *d2h_bytes)
+{
+    if (!S) return fail(RTM_ERR_INVALID, "null stack");
+    if (d2h_copies) *d2h_copies = S->d2h_copies;
+    if (d2h_bytes) *d2h_bytes = S->d2h_bytes;
+    return RTM_OK;
+}
+
 void rtm_release_cached(void)
 {
     std::lock_guard<std::mutex> lk(g_mu);

@@ -256,5 +256,9 @@ cudaError_t launch_laplacian(int nx, int nz, const float *in, float *out, cudaSt
 template <typename T>
 cudaError_t launch_xcorr(const Geom &g, const T *src, const T *rcv, double *img, double *slf,
                          cudaStream_t s);
+cudaError_t launch_stack_add(const Geom &g, const double *img, const double *slf, float *acc_img,
+                             float *acc_slf, unsigned *plan_status, unsigned *stack_status, cudaStream_t s);
+cudaError_t launch_stack_finish(int n, const float *acc_img, const float *acc_slf, int normalize, float *out,
+                                cudaStream_t s);
 
 }  // namespace rtm

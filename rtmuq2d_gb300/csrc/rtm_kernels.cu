@@ -461,6 +461,45 @@ __global__ void k_laplacian(int nx, int nz, const float *in, float *out)
         + RTM_AC4 * (((c[-4 * s] + c[4 * s]) + c[-4]) + c[4]);
 }
 
+// Shot stack on the device (SRC/rtm_iso2d.c:121-126): stack = stack + (float)image, in the
+// reference's float arithmetic (the per-shot image rounded to float, then a float sum).  The
+// plan's status word is folded into the stack's and cleared, so that a failure of any shot
+// surfaces when the stack is read.
+__global__ void k_stack_add(Geom g, const double *img, const double *slf, float *acc_img,
+                            float *acc_slf, unsigned *plan_status, unsigned *stack_status)
+{
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = blockIdx.y;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        const unsigned s = *plan_status;
+        if (s) {
+            atomicOr(stack_status, s);
+            *plan_status = 0;
+        }
+    }
+    if (z >= g.nz || x >= g.nx) return;
+    const size_t i = (size_t)x * g.nz + z;
+    const size_t o = (size_t)x * g.pitch + g.thu + z;
+    acc_img[i] = acc_img[i] + (float)img[o];
+    acc_slf[i] = acc_slf[i] + (float)slf[o];
+}
+
+// The stacked image as the driver writes it: the image stack, or (normalize) the image stack
+// divided by the self-image stack (rtm_iso2d.c:150-156, float division), where a pixel with a
+// zero self-image stack -- no source energy reached it -- is set to 0 instead of 0/0 or x/0.
+__global__ void k_stack_finish(int n, const float *acc_img, const float *acc_slf, int normalize, float *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = acc_img[i];
+    if (!normalize) {
+        out[i] = v;
+        return;
+    }
+    const float s = acc_slf[i];
+    out[i] = s != 0.0f ? v / s : 0.0f;
+}
+
 template <typename T>
 __global__ void k_xcorr(Geom g, const T *src, const T *rcv, double *img, double *slf)
 {
@@ -652,6 +691,21 @@ cudaError_t launch_laplacian(int nx, int nz, const float *in, float *out, cudaSt
 {
     dim3 grid((nz + 127) / 128, nx);
     k_laplacian<<<grid, 128, 0, s>>>(nx, nz, in, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stack_add(const Geom &g, const double *img, const double *slf, float *acc_img,
+                             float *acc_slf, unsigned *plan_status, unsigned *stack_status, cudaStream_t s)
+{
+    dim3 grid((g.nz + 127) / 128, g.nx);
+    k_stack_add<<<grid, 128, 0, s>>>(g, img, slf, acc_img, acc_slf, plan_status, stack_status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stack_finish(int n, const float *acc_img, const float *acc_slf, int normalize, float *out,
+                                cudaStream_t s)
+{
+    k_stack_finish<<<(n + 255) / 256, 256, 0, s>>>(n, acc_img, acc_slf, normalize, out);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,65 @@ def test_routine_matches_reference(engine, tmp_path, storage):
     st, lp = _outputs(d, tmp_path, sim_id)
     assert rel_l2(st, d["routine/stacked"]) <= 1e-4
     assert rel_l2(lp, d["routine/laplacian"]) <= 1e-4
+    # the shots are stacked on the device: one copy back (stack, Laplacian, status word)
+    assert engine.routine_last_transfers() == (1, 2 * p.nx * p.nz * 4 + 4)
+
+
+def test_device_stack_equals_host_stack(engine, tmp_path):
+    """rtm_stack: the shots' images added on the device in shot order equal, bit for bit, the
+    host-side sum of the same shots' images from rtm_adjoint_modeling (float32, shot order, as
+    rtm_iso2d.c:121-126 sums them), and its Laplacian equals laplacian_filter2D of that sum;
+    one device-to-host copy for the whole stack."""
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    _, n_shots, first, spacing, depth = (int(v) for v in d["routine/survey"])
+    tol = float(d["routine/tol"][0])
+    ext = engine.extend_matrix(p, d["uneven/model"])
+    wav = d["uneven/wavelet"]
+    host_img = np.zeros((p.nx, p.nz), np.float32)
+    host_slf = np.zeros((p.nx, p.nz), np.float32)
+    stack = engine.Stack(p)
+    for k in range(n_shots):
+        shot = (first + k * spacing, depth)
+        seis = engine.zfp_decode(d["routine/seis_%d" % (k + 1)].tobytes(), p.rec_count, p.nt, tol)
+        img = np.zeros((p.nx, p.nz), np.float32)
+        slf = np.zeros((p.nx, p.nz), np.float32)
+        engine.forward_modeling(p, 5, shot, ext, wav)
+        engine.adjoint_modeling(p, 5, shot, ext, wav, seis, img, slf)
+        host_img = host_img + img
+        host_slf = host_slf + slf
+        engine.forward_modeling(p, 6, shot, ext, wav)
+        stack.adjoint(p.replace(shot_x=shot[0], shot_z=shot[1]), 6, shot, seis)
+    out, lap = stack.finish()
+    assert stack.transfers() == (1, 2 * p.nx * p.nz * 4 + 4)
+    assert np.array_equal(out, host_img)
+    assert np.array_equal(lap, engine.laplacian_filter2D(p, host_img))
+    raw_img, raw_slf = stack.read_raw()
+    assert np.array_equal(raw_img, host_img) and np.array_equal(raw_slf, host_slf)
+    norm, _ = stack.finish(normalize_by_self=True)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        want = np.where(host_slf != 0, host_img / host_slf, np.float32(0)).astype(np.float32)
+    assert np.array_equal(norm, want)
+    stack.close()
+
+
+def test_stack_normalization_zero_guard(engine):
+    """A pixel whose self-image stack is 0 (no source energy reached it) is 0 in the normalised
+    stack, not the 0/0 or x/0 of the reference's commented-out division; every other pixel is
+    the float quotient."""
+    d = load()
+    p = engine.RtmParams.make(**case_params(d, "uneven"))
+    rng = np.random.default_rng(4)
+    img = rng.standard_normal((p.nx, p.nz)).astype(np.float32)
+    slf = np.abs(rng.standard_normal((p.nx, p.nz))).astype(np.float32)
+    slf[:, : p.nz // 3] = 0.0                      # a shadow zone
+    img[: p.nx // 2, : p.nz // 3] = 0.0           # 0/0 there, x/0 beside it
+    stack = engine.Stack(p)
+    stack.load(img, slf)
+    out, lap = stack.finish(normalize_by_self=True)
+    stack.close()
+    assert np.isfinite(out).all() and np.isfinite(lap).all()
+    assert not np.any(out[:, : p.nz // 3])
+    assert np.array_equal(out[:, p.nz // 3:], img[:, p.nz // 3:] / slf[:, p.nz // 3:])
 
 
 def test_dropin_rtm_routine_matches_reference(engine, tmp_path):
@@ -150,3 +209,36 @@ def test_routine_resumes_from_its_checkpoint(engine, tmp_path):
     got = _outputs(d, tmp_path, sim_id)
     assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
     assert not ckpt.exists()
+    # with a checkpoint file, the stacks come back after each shot too
+    assert engine.routine_last_transfers()[0] == 1 + (s.n_shots - 1)
+
+
+def test_routine_ignores_a_checkpoint_of_another_survey(engine, tmp_path):
+    """A checkpoint left by a survey of the same shape but another shot geometry is not
+    resumed: the run starts from zero stacks and writes what an uninterrupted run writes."""
+    d, p, s, sim_id = _setup(engine, tmp_path)
+    ck = str(tmp_path / "OUTPUTS" / "stack_%05d.ckpt")
+
+    def survey(first_shot):
+        return engine.RtmSurvey.make(*(getattr(s, k).decode() for k in ("velocity_file", "wavelet_file",
+                                                                          "seismogram_file", "stacked_file",
+                                                                          "laplacian_file")),
+                                     first_shot=first_shot, shot_depth=s.shot_depth,
+                                     shot_spacing=s.shot_spacing, n_shots=s.n_shots,
+                                     zfp_tolerance=s.zfp_tolerance, checkpoint_file=ck)
+
+    other = survey(s.first_shot + 2)
+    seis2 = tmp_path / "INPUTS" / "seismogram_00002.zfp"
+    hidden = tmp_path / "seismogram_00002.zfp"
+    seis2.rename(hidden)
+    with pytest.raises(engine.RtmError):
+        engine.routine_run(p, other, sim_id)       # leaves a checkpoint after its shot 1
+    assert os.path.exists(ck % sim_id)
+    hidden.rename(seis2)
+    engine.routine_run(p, survey(s.first_shot), sim_id)
+    got = _outputs(d, tmp_path, sim_id)
+    for f in (tmp_path / "OUTPUTS").iterdir():
+        f.unlink()
+    engine.routine_run(p, s, sim_id)
+    want = _outputs(d, tmp_path, sim_id)
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
