@@ -91,14 +91,14 @@ static EncodeTiledFn tensor_map_encoder()
     return fn;
 }
 
-// 2-D map over a pitched field: dims {pitch (z), dimx (x)}, box {SZ, tx+8}, zero fill.
-static int make_field_map(CUtensorMap *m, void *base, const Geom &g, size_t es)
+// 2-D map over a pitched field: dims {pitch (z), dimx (x)}, box {SZ, tx + 2 xhalo}, zero fill.
+static int make_field_map(CUtensorMap *m, void *base, const Geom &g, size_t es, int xhalo = HALO)
 {
     EncodeTiledFn enc = tensor_map_encoder();
     if (!enc) return fail(RTM_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
     cuuint64_t dims[2] = {(cuuint64_t)g.pitch, (cuuint64_t)g.dimx};
     cuuint64_t strides[1] = {(cuuint64_t)g.pitch * es};
-    cuuint32_t box[2] = {(cuuint32_t)SZ, (cuuint32_t)(g.tx + 2 * HALO)};
+    cuuint32_t box[2] = {(cuuint32_t)SZ, (cuuint32_t)(g.tx + 2 * xhalo)};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                      2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -170,14 +170,28 @@ static Geom make_geom(const rtm_params &p, bool batched = false)
     // it, the receiver row and the shot, so that every other top tile is plain interior
     if (batched) {
         g.ztop = TZ;
+        g.zbot = 0;
+        g.tiles_z = g.dimz <= g.ztop ? 1 : 1 + (g.dimz - g.ztop + TZ - 1) / TZ;
     } else {
-        int top = g.thu - 4;
-        if (g.zrec < g.thu + 16) top = std::max(top, g.zrec + 1);
-        if (g.zs < g.thu + 16) top = std::max(top, g.zs + 1);
-        g.ztop = std::min(TZ, std::max(4, round_up(top, 4)));
-        if (g.ztop >= g.dimz) g.ztop = std::min(TZ, round_up(g.dimz, 4));
+        // the last z-tile starts at the 4-aligned row at or above the bottom CPML band, so
+        // that each band (plus 4 rows inward) lies inside one z-tile: the fused CPML update
+        // rebuilds psi in the tile from the tile's own rows
+        if (g.dimz <= TZ) {
+            g.ztop = round_up(g.dimz, 4);
+            g.zbot = 0;
+            g.tiles_z = 1;
+        } else {
+            int top = g.thu - 4;
+            if (g.zrec < g.thu + 16) top = std::max(top, g.zrec + 1);
+            if (g.zs < g.thu + 16) top = std::max(top, g.zs + 1);
+            g.ztop = std::min(TZ, std::max(4, round_up(top, 4)));
+            // uniform TZ-row tiles below the top one, when the last of them holds the bottom
+            // band; otherwise the last tile starts at the band and the one above it is short
+            const int last = g.ztop + (g.dimz - g.ztop - 1) / TZ * TZ;
+            g.zbot = last <= ((g.dimz - g.thd) & ~3) ? last : std::max(g.ztop, (g.dimz - g.thd) & ~3);
+            g.tiles_z = 2 + (g.zbot - g.ztop + TZ - 1) / TZ;
+        }
     }
-    g.tiles_z = g.dimz <= g.ztop ? 1 : 1 + (g.dimz - g.ztop + TZ - 1) / TZ;
     g.tiles = g.tiles_x * g.tiles_z;
     g.nxl = std::min(g.tiles_x, (g.thl - 4 + g.tx - 1) / g.tx);
     g.xr0 = std::max(g.nxl, std::min(g.tiles_x, (g.dimx - g.thr + 4) / g.tx));
@@ -186,9 +200,11 @@ static Geom make_geom(const rtm_params &p, bool batched = false)
 
 static int check_params(const rtm_params &p)
 {
-    if (p.nx < 1 || p.nz < 1) return fail(RTM_ERR_INVALID, "nx, nz must be >= 1");
+    if (p.nx < 1 || p.nz < 4) return fail(RTM_ERR_INVALID, "nx must be >= 1 and nz >= 4");
     if (p.th_left < 12 || p.th_right < 12 || p.th_up < 12 || p.th_down < 12)
         return fail(RTM_ERR_INVALID, "every CPML thickness must be >= 12 cells");
+    if (p.th_up > kMaxStripThickness || p.th_down > kMaxStripThickness)
+        return fail(RTM_ERR_INVALID, "top and bottom CPML thickness must be <= %d cells", kMaxStripThickness);
     if (!(p.dx > 0.0f) || !(p.dt > 0.0f)) return fail(RTM_ERR_INVALID, "dx and dt must be > 0");
     if (p.nt < 1) return fail(RTM_ERR_INVALID, "nt must be >= 1");
     if (p.n_wavelet < 0) return fail(RTM_ERR_INVALID, "n_wavelet must be >= 0");
@@ -234,6 +250,7 @@ struct Layout {
     size_t u[2], r[2], coef, strips, strip_bytes, prof, rec, wav, seis_t, img, slf, store,
         store_bytes, scales, staging, status, total;
     size_t psi[4], xi[4];
+    size_t psn[4];       // the second psi buffer (a step reads one psi buffer, writes the other)
     int nslots;
     size_t slot_elems;   // elements per storage slot
     size_t n_scales_per_slot;
@@ -299,6 +316,7 @@ static Layout make_layout(const rtm_params &p, const Geom &g)
     L.strips = off;
     L.psi[0] = take(n_l * es); L.psi[1] = take(n_r * es); L.psi[2] = take(n_t * es); L.psi[3] = take(n_b * es);
     L.xi[0] = take(n_l * es); L.xi[1] = take(n_r * es); L.xi[2] = take(n_t * es); L.xi[3] = take(n_b * es);
+    L.psn[0] = take(n_l * es); L.psn[1] = take(n_r * es); L.psn[2] = take(n_t * es); L.psn[3] = take(n_b * es);
     L.strip_bytes = off - L.strips;
     L.prof = take(sizeof(float) * (size_t)prof_layout(g).total);
     L.rec = take(sizeof(int) * 3 * (size_t)g.dimx);
@@ -326,6 +344,12 @@ static Layout make_layout(const rtm_params &p, const Geom &g)
     return L;
 }
 
+// A profiled block of consecutive step-kernel launches: its events and launch count.
+struct ProfBlock {
+    cudaEvent_t e0, e1;
+    int launches;
+};
+
 // ---- plan ---------------------------------------------------------------------------------
 }  // namespace rtm
 
@@ -338,6 +362,7 @@ struct rtm_plan {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     CUtensorMap tm_u[2], tm_r[2];      // halo maps (box tx+8 x 136) of u[], r[]
+    CUtensorMap tm_u8[2], tm_r8[2];    // 8-column x halo maps (box tx+16 x 136): side CPML tiles
     CUtensorMap tm_up[2], tm_rp[2];    // plain maps (box tx x 128) of u[], r[]
     CUtensorMap tm_c;                  // plain map of coef
     int cur_u = 0;        // u buffer holding u_nt after the forward pass
@@ -348,18 +373,21 @@ struct rtm_plan {
     std::vector<float> h_prof;
     float *h_pinned = nullptr;   // pinned staging for host-buffer entry points
     size_t h_pinned_bytes = 0;
-    // sampled per-launch timing of k_step (CUDA events on the plan's stream)
+    // sampled timing of k_step: blocks of consecutive launches bracketed by CUDA events on
+    // the plan's stream
     int prof_every = 0;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_launch[2];   // [forward, backward]
+    std::vector<rtm::ProfBlock> prof_launch[2];   // [forward, backward]
+    cudaEvent_t prof_e0 = nullptr;     // the open block's start event
+    int prof_n = 0;                    // launches in the open block
     // CUDA graphs of the two time loops, captured on first use and replayed afterwards
     bool use_graphs = true;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int graph_key[2] = {-1, -1};
     long long graph_launches[2] = {0, 0};
     int capture_pass = -1;       // pass being captured (0 forward, 1 backward), or -1
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> graph_events[2];
+    std::vector<rtm::ProfBlock> graph_events[2];
     // source-field captures of the next adjoint pass (rtm_plan_capture_source)
     std::vector<int> cap_times;
     void *cap_out = nullptr;
@@ -401,6 +429,8 @@ static int make_maps(rtm_plan *P)
     for (int i = 0; i < 2; ++i) {
         RTM_TRY(make_field_map(&P->tm_u[i], P->base + P->L.u[i], P->g, P->es));
         RTM_TRY(make_field_map(&P->tm_r[i], P->base + P->L.r[i], P->g, P->es));
+        RTM_TRY(make_field_map(&P->tm_u8[i], P->base + P->L.u[i], P->g, P->es, 2 * HALO));
+        RTM_TRY(make_field_map(&P->tm_r8[i], P->base + P->L.r[i], P->g, P->es, 2 * HALO));
         RTM_TRY(make_plain_map(&P->tm_up[i], P->base + P->L.u[i], P->g, P->es));
         RTM_TRY(make_plain_map(&P->tm_rp[i], P->base + P->L.r[i], P->g, P->es));
     }
@@ -456,7 +486,7 @@ static void plan_free(rtm_plan *P)
     for (cudaEvent_t e : P->ev_pool) cudaEventDestroy(e);
     for (int k = 0; k < 2; ++k) {
         if (P->gexec[k]) cudaGraphExecDestroy(P->gexec[k]);
-        for (auto &pr : P->graph_events[k]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        for (auto &pb : P->graph_events[k]) { cudaEventDestroy(pb.e0); cudaEventDestroy(pb.e1); }
     }
     if (P->own_stream && P->stream) cudaStreamDestroy(P->stream);
     delete P;
@@ -475,6 +505,17 @@ static int pinned(rtm_plan *P, size_t bytes, float **out)
     return RTM_OK;
 }
 
+// psi buffers of step t: it reads set (t+1) & 1 (the previous step's psi) and writes set t & 1,
+// set 0 = L.psi, set 1 = L.psn.
+template <typename T>
+static void set_psi_parity(rtm_plan *P, StepArgs<T> &a, int t)
+{
+    const size_t *rd = (t & 1) ? P->L.psi : P->L.psn;
+    const size_t *wr = (t & 1) ? P->L.psn : P->L.psi;
+    a.psi_l = P->at<T>(rd[0]); a.psi_r = P->at<T>(rd[1]); a.psi_t = P->at<T>(rd[2]); a.psi_b = P->at<T>(rd[3]);
+    a.psn_l = P->at<T>(wr[0]); a.psn_r = P->at<T>(wr[1]); a.psn_t = P->at<T>(wr[2]); a.psn_b = P->at<T>(wr[3]);
+}
+
 template <typename T>
 static void fill_common(rtm_plan *P, StepArgs<T> &a)
 {
@@ -485,8 +526,7 @@ static void fill_common(rtm_plan *P, StepArgs<T> &a)
     a.h1 = (T)1.0f / dx;
     a.h2 = dx * dx;
     a.h3 = (T)1.0f / (dx * dx);
-    a.psi_l = P->at<T>(P->L.psi[0]); a.psi_r = P->at<T>(P->L.psi[1]);
-    a.psi_t = P->at<T>(P->L.psi[2]); a.psi_b = P->at<T>(P->L.psi[3]);
+    set_psi_parity<T>(P, a, 0);
     a.xi_l = P->at<T>(P->L.xi[0]); a.xi_r = P->at<T>(P->L.xi[1]);
     a.xi_t = P->at<T>(P->L.xi[2]); a.xi_b = P->at<T>(P->L.xi[3]);
     const float *prof = P->at<float>(P->L.prof);
@@ -501,19 +541,6 @@ static void fill_common(rtm_plan *P, StepArgs<T> &a)
     a.status = P->at<unsigned>(P->L.status);
 }
 
-template <typename T>
-static void fill_psi(rtm_plan *P, const StepArgs<T> &a, PsiArgs<T> &q)
-{
-    memset(&q, 0, sizeof q);
-    q.g = a.g;
-    q.h1 = a.h1;
-    q.psi_l = const_cast<T *>(a.psi_l); q.psi_r = const_cast<T *>(a.psi_r);
-    q.psi_t = const_cast<T *>(a.psi_t); q.psi_b = const_cast<T *>(a.psi_b);
-    q.a_l = a.a_l; q.b_l = a.b_l; q.a_r = a.a_r; q.b_r = a.b_r;
-    q.a_t = a.a_t; q.b_t = a.b_t; q.a_b = a.a_b; q.b_b = a.b_b;
-    (void)P;
-}
-
 static void *slot_ptr(rtm_plan *P, int slot)
 {
     const size_t se = P->p.precision == RTM_PREC_FP32 ? P->es : 2;
@@ -526,42 +553,55 @@ static float *scale_ptr(rtm_plan *P, int slot)
     return P->at<float>(P->L.scales) + (size_t)slot * P->L.n_scales_per_slot;
 }
 
-// Steps whose k_step launch is bracketed by profiling events (no programmatic overlap
-// across an event record).
-static bool sampled(const rtm_plan *P, int step)
+// Launches per profiled block: with profiling on (prof_every > 0), the step kernels of steps
+// [k every, k every + kProfBlock) are bracketed together by one pair of CUDA events, so that
+// the launches inside a block keep their programmatic overlap; the block's time over its
+// launches is their average launch duration.
+constexpr int kProfBlock = 8;
+
+static cudaEvent_t prof_event(rtm_plan *P)
 {
-    return P->prof_every > 0 && step % P->prof_every == 0;
+    cudaEvent_t e = nullptr;
+    if (P->capture_pass >= 0) {          // events owned by the graph being captured
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        return e;
+    }
+    return P->next_event();
 }
 
-// k_step launch, bracketed by CUDA events on sampled steps when profiling is on.
+// One k_step launch of a pass of `steps` steps, inside a profiled block when profiling is on.
+// Consecutive step kernels chain by programmatic dependent launch, except right after an
+// event record.
 template <typename T>
-static int timed_step(rtm_plan *P, int backward, int step, const StepMaps &maps,
+static int timed_step(rtm_plan *P, int backward, int step, int steps, const StepMaps &maps,
                       const StepArgs<T> &a)
 {
-    const bool sample = sampled(P, step);
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (sample) {
-        if (P->capture_pass >= 0) {      // events owned by the graph being captured
-            RTM_CUDA(cudaEventCreate(&e0));
-            RTM_CUDA(cudaEventCreate(&e1));
-        } else {
-            e0 = P->next_event();
-            e1 = P->next_event();
-        }
-        if (!e0 || !e1) return fail(RTM_ERR_CUDA, "event pool");
+    const int every = P->prof_every;
+    const int block = every > 0 ? std::min(kProfBlock, every) : 0;
+    const bool opens = every > 0 && step % every == 0;
+    const bool closes = every > 0 && step % every < block && (step % every == block - 1 || step == steps - 1);
+    const unsigned rec_flags = P->capture_pass >= 0 ? cudaEventRecordExternal : 0;
+    bool after_event = step == 0;
+    if (opens) {
+        P->prof_e0 = prof_event(P);
+        if (!P->prof_e0) return fail(RTM_ERR_CUDA, "event pool");
         // inside a capture, an external event-record node keeps the event timeable
-        RTM_CUDA(cudaEventRecordWithFlags(e0, P->stream,
-                                          P->capture_pass >= 0 ? cudaEventRecordExternal : 0));
+        RTM_CUDA(cudaEventRecordWithFlags(P->prof_e0, P->stream, rec_flags));
+        P->prof_n = 0;
+        after_event = true;
     }
+    if (every > 0 && step > 0 && (step - 1) % every == block - 1) after_event = true;   // a block closed
     const int grid = step_grid<T>(backward, P->g);
     if (grid < 1) return fail(RTM_ERR_CUDA, "step kernel cannot be configured (tile_x %d)", P->g.tx);
-    // programmatic dependent launch: the step kernel overlaps the psi kernel before it
-    RTM_CUDA(launch_step<T>(backward, maps, a, grid, sample ? 0 : 1, P->stream));
-    if (sample) {
-        RTM_CUDA(cudaEventRecordWithFlags(e1, P->stream,
-                                          P->capture_pass >= 0 ? cudaEventRecordExternal : 0));
-        if (P->capture_pass >= 0) P->graph_events[P->capture_pass].push_back({e0, e1});
-        else P->prof_launch[backward ? 1 : 0].push_back({e0, e1});
+    RTM_CUDA(launch_step<T>(backward, maps, a, grid, after_event ? 0 : 1, P->stream));
+    P->prof_n++;
+    if (closes) {
+        cudaEvent_t e1 = prof_event(P);
+        if (!e1) return fail(RTM_ERR_CUDA, "event pool");
+        RTM_CUDA(cudaEventRecordWithFlags(e1, P->stream, rec_flags));
+        const ProfBlock pb{P->prof_e0, e1, P->prof_n};
+        if (P->capture_pass >= 0) P->graph_events[P->capture_pass].push_back(pb);
+        else P->prof_launch[backward ? 1 : 0].push_back(pb);
     }
     return RTM_OK;
 }
@@ -577,7 +617,7 @@ static int run_loop(rtm_plan *P, int which, bool graphable, F issue)
     if (!P->gexec[which] || P->graph_key[which] != key) {
         if (P->gexec[which]) cudaGraphExecDestroy(P->gexec[which]);
         P->gexec[which] = nullptr;
-        for (auto &pr : P->graph_events[which]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+        for (auto &pb : P->graph_events[which]) { cudaEventDestroy(pb.e0); cudaEventDestroy(pb.e1); }
         P->graph_events[which].clear();
         const long long before = P->launches;
         RTM_CUDA(cudaStreamBeginCapture(P->stream, cudaStreamCaptureModeThreadLocal));
@@ -625,53 +665,39 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
     fill_common<T>(P, a);
     a.wavelet = d_wav;
     a.rec_out = d_seis_out;
-    PsiArgs<T> q;
-    fill_psi<T>(P, a, q);
     const bool ring = P->p.storage == RTM_STORE_RING;
-    // FP32 rings are saved by the psi kernel of the next step (slot t holds u_t), the last one
-    // by a ring-only pass after the loop; 16-bit rings by the step kernel (per-tile scales)
-    const bool ring_psi = ring && P->p.precision == RTM_PREC_FP32;
     (void)step_grid<T>(0, g);            // configure the kernels before any capture
     auto loop = [&]() -> int {
         int c = 0;
         StepMaps maps;
         for (int t = 0; t < g.nt; ++t) {
-            q.u = u[c];
-            q.ring = ring_psi && t >= 1 ? static_cast<T *>(slot_ptr(P, t)) : nullptr;
-            RTM_CUDA(launch_psi<T>(q, t > 0 && !sampled(P, t - 1), s));
             a.u_next = u[1 - c];
             a.t = t;
+            set_psi_parity<T>(P, a, t);
             int f = 0;
             if (t < g.nwav) f |= F_SRC;
             if (d_seis_out && g.nrec > 0) f |= F_RECORD;
             a.store = nullptr;
             a.store_scale = nullptr;
-            if (ring && !ring_psi) {
+            if (ring) {                  // slot t + 1 holds the ring of u_{t+1}
                 f |= F_RING_SAVE;
                 a.store = slot_ptr(P, t + 1);
                 a.store_scale = scale_ptr(P, t + 1);
-            } else if (!ring && t % g.slices == 0) {
+            } else if (t % g.slices == 0) {
                 f |= F_SNAP_SAVE;
                 a.store = slot_ptr(P, t / g.slices);
                 a.store_scale = scale_ptr(P, t / g.slices);
             }
             a.flags = f;
             maps.cur = P->tm_u[c];
+            maps.cur8 = P->tm_u8[c];
             maps.prev = P->tm_up[1 - c];
             maps.coef = P->tm_c;
             maps.scur = P->tm_u[c];
             maps.sprev = P->tm_up[1 - c];
-            RTM_TRY(timed_step<T>(P, 0, t, maps, a));
-            P->launches += 2;
+            RTM_TRY(timed_step<T>(P, 0, t, g.nt, maps, a));
+            P->launches += 1;
             c ^= 1;
-        }
-        if (ring_psi) {                  // the ring of u_nt
-            PsiArgs<T> r = q;
-            r.u = u[c];
-            r.ring = static_cast<T *>(slot_ptr(P, g.nt));
-            r.ring_only = 1;
-            RTM_CUDA(launch_psi<T>(r, !sampled(P, g.nt - 1), s));
-            P->launches++;
         }
         return RTM_OK;
     };
@@ -718,8 +744,6 @@ static int run_adjoint(rtm_plan *P, const float *d_seis)
     StepArgs<T> a;
     fill_common<T>(P, a);
     a.wavelet = P->at<float>(P->L.wav);
-    PsiArgs<T> q;
-    fill_psi<T>(P, a, q);
     const bool ring = P->p.storage == RTM_STORE_RING;
     const int ua = P->cur_u, ub = 1 - P->cur_u;   // u_nt, u_{nt-1}
     (void)step_grid<T>(1, g);            // configure the kernels before any capture
@@ -777,17 +801,17 @@ static int run_adjoint(rtm_plan *P, const float *d_seis)
                 ctrl--;
             }
             a.flags = f;
-            q.u = r[c];
-            RTM_CUDA(launch_psi<T>(q, time > 0 && !sampled(P, time - 1), s));
             a.u_next = r[1 - c];
+            set_psi_parity<T>(P, a, time);
             StepMaps maps;
             maps.cur = P->tm_r[c];
+            maps.cur8 = P->tm_r8[c];
             maps.prev = P->tm_rp[1 - c];
             maps.coef = P->tm_c;
             maps.scur = P->tm_u[sc];
             maps.sprev = P->tm_up[sp];
-            RTM_TRY(timed_step<T>(P, 1, time, maps, a));
-            P->launches += 2;
+            RTM_TRY(timed_step<T>(P, 1, time, g.nt, maps, a));
+            P->launches += 1;
             c ^= 1;
             if (recon && !P->cap_times.empty()) RTM_TRY(capture(g.nt - time, u[sp]));
             if (recon) std::swap(sc, sp);
@@ -1128,16 +1152,18 @@ int rtm_plan_profile_read(rtm_plan *plan, double *fwd_ms, int *fwd_n, double *bw
     if (!plan) return fail(RTM_ERR_INVALID, "null plan");
     RTM_CUDA(cudaStreamSynchronize(plan->stream));
     double ms[2] = {0.0, 0.0};
+    int n[2] = {0, 0};
     for (int k = 0; k < 2; ++k)
-        for (auto &pr : plan->prof_launch[k]) {
+        for (auto &pb : plan->prof_launch[k]) {
             float v = 0.0f;
-            RTM_CUDA(cudaEventElapsedTime(&v, pr.first, pr.second));
+            RTM_CUDA(cudaEventElapsedTime(&v, pb.e0, pb.e1));
             ms[k] += v;
+            n[k] += pb.launches;
         }
     if (fwd_ms) *fwd_ms = ms[0];
-    if (fwd_n) *fwd_n = (int)plan->prof_launch[0].size();
+    if (fwd_n) *fwd_n = n[0];
     if (bwd_ms) *bwd_ms = ms[1];
-    if (bwd_n) *bwd_n = (int)plan->prof_launch[1].size();
+    if (bwd_n) *bwd_n = n[1];
     plan->ev_used = 0;
     plan->prof_launch[0].clear();
     plan->prof_launch[1].clear();
@@ -1473,15 +1499,18 @@ static int field_to_host(rtm_plan *P, float *dst, const float *src)
     return RTM_OK;
 }
 
-// strip arrays between the reference layouts and the pitched device layouts
+// strip arrays between the reference layouts and the pitched device layouts.  A one-step
+// plan's step (t = 0) reads psi from the second buffer (L.psn) and writes it to the first
+// (L.psi): psi goes up to L.psn and comes back from L.psi.
 static int strips_io(rtm_plan *P, int to_device, float *const host[8])
 {
     const Geom &g = P->g;
     // the bottom strip's reference rows start at z = dimZ - th_down, the device rows at zb0
     const size_t bsh = (size_t)((g.dimz - g.thd) - g.zb0);
+    const size_t *psi = to_device ? P->L.psn : P->L.psi;
     struct { size_t off; int rows, host_w, dev_w; size_t shift; } s[8] = {
-        {P->L.psi[0], g.thl, g.dimz, g.pitch, 0}, {P->L.psi[1], g.thr, g.dimz, g.pitch, 0},
-        {P->L.psi[2], g.dimx, g.thu, g.st, 0},    {P->L.psi[3], g.dimx, g.thd, g.sb, bsh},
+        {psi[0], g.thl, g.dimz, g.pitch, 0}, {psi[1], g.thr, g.dimz, g.pitch, 0},
+        {psi[2], g.dimx, g.thu, g.st, 0},    {psi[3], g.dimx, g.thd, g.sb, bsh},
         {P->L.xi[0], g.thl, g.dimz, g.pitch, 0},  {P->L.xi[1], g.thr, g.dimz, g.pitch, 0},
         {P->L.xi[2], g.dimx, g.thu, g.st, 0},     {P->L.xi[3], g.dimx, g.thd, g.sb, bsh}};
     for (int i = 0; i < 8; ++i) {
@@ -1491,6 +1520,12 @@ static int strips_io(rtm_plan *P, int to_device, float *const host[8])
             RTM_CUDA(cudaMemsetAsync(row0, 0, (size_t)s[i].rows * s[i].dev_w * sizeof(float), P->stream));
             RTM_CUDA(cudaMemcpy2DAsync(dev, s[i].dev_w * sizeof(float), host[i], s[i].host_w * sizeof(float),
                                        s[i].host_w * sizeof(float), s[i].rows, cudaMemcpyHostToDevice, P->stream));
+            if (i < 4) {                  // psi: the written buffer starts as the input, so that
+                                          // the cells the step does not update come back as given
+                unsigned char *w0 = P->base + P->L.psi[i];
+                RTM_CUDA(cudaMemcpyAsync(w0, row0, (size_t)s[i].rows * s[i].dev_w * sizeof(float),
+                                         cudaMemcpyDeviceToDevice, P->stream));
+            }
         } else {
             RTM_CUDA(cudaMemcpy2DAsync(host[i], s[i].host_w * sizeof(float), dev, s[i].dev_w * sizeof(float),
                                        s[i].host_w * sizeof(float), s[i].rows, cudaMemcpyDeviceToHost, P->stream));
@@ -1500,21 +1535,16 @@ static int strips_io(rtm_plan *P, int to_device, float *const host[8])
     return RTM_OK;
 }
 
-static int one_step(rtm_plan *P, int flags, bool with_psi)
+// One step of u[0] into u[1] (t = 0: psi read from L.psn, written to L.psi; see strips_io).
+static int one_step(rtm_plan *P, int flags)
 {
     StepArgs<float> a;
     fill_common<float>(P, a);
     a.u_next = P->at<float>(P->L.u[1]);
     a.flags = flags;
-    if (with_psi) {
-        PsiArgs<float> q;
-        fill_psi<float>(P, a, q);
-        q.u = P->at<float>(P->L.u[0]);
-        RTM_CUDA(launch_psi<float>(q, 0, P->stream));
-        P->launches++;
-    }
     StepMaps maps;
     maps.cur = P->tm_u[0];
+    maps.cur8 = P->tm_u8[0];
     maps.prev = P->tm_up[1];
     maps.coef = P->tm_c;
     maps.scur = P->tm_u[0];
@@ -1537,7 +1567,7 @@ int rtm_iso_acoustic_wave_equation(const rtm_params *p, const float *pond, const
     int st = field_from_host(P, P->at<float>(P->L.coef), pond);
     if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[0]), wave2);
     if (st == RTM_OK) st = field_from_host(P, P->at<float>(P->L.u[1]), wave3);
-    if (st == RTM_OK) st = one_step(P, F_NO_CPML, false);
+    if (st == RTM_OK) st = one_step(P, F_NO_CPML);
     if (st == RTM_OK) st = field_to_host(P, wave3, P->at<float>(P->L.u[1]));
     release_plan(P);
     return st;
@@ -1566,7 +1596,7 @@ int rtm_aiso_attenuation_cpml(const rtm_params *p, const float *wave1, float *wa
     if (st == RTM_OK && cudaMemcpy(P->base + P->L.prof, prof.data(), prof.size() * sizeof(float),
                                    cudaMemcpyHostToDevice) != cudaSuccess)
         st = fail(RTM_ERR_CUDA, "profile upload");
-    if (st == RTM_OK) st = one_step(P, F_NO_STENCIL, true);
+    if (st == RTM_OK) st = one_step(P, F_NO_STENCIL);
     if (st == RTM_OK) st = field_to_host(P, wave2, P->at<float>(P->L.u[1]));
     if (st == RTM_OK) st = strips_io(P, 0, strips);
     cudaMemcpy(P->base + P->L.prof, P->h_prof.data(), P->h_prof.size() * sizeof(float),

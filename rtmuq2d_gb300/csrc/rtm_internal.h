@@ -55,6 +55,8 @@ struct Geom {
     int tx;                     // x columns per tile
     int ztop;                   // height of z-tile 0 (4-aligned, <= TZ): the top CPML band;
                                 // z-tile k >= 1 starts at ztop + (k-1)*TZ
+    int zbot;                   // > 0: the last z-tile is [zbot, dimz) (4-aligned, holds the
+                                // bottom CPML band), the ones before it end at zbot at most
     int tiles_x, tiles_z, tiles;
     int nxl, xr0;               // left CPML x-tiles [0,nxl), right ones [xr0,tiles_x)
 };
@@ -107,10 +109,17 @@ __host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
 
 __host__ __device__ __forceinline__ int ztile_origin(const Geom &g, int zt)
 {
-    return zt == 0 ? 0 : g.ztop + (zt - 1) * TZ;
+    if (zt == 0) return 0;
+    if (g.zbot > 0 && zt == g.tiles_z - 1) return g.zbot;
+    return g.ztop + (zt - 1) * TZ;
 }
 __host__ __device__ __forceinline__ int ztile_end(const Geom &g, int zt)
 {
+    if (g.zbot > 0) {
+        if (zt == g.tiles_z - 1) return g.dimz;
+        const int e = zt == 0 ? g.ztop : g.ztop + zt * TZ;
+        return e < g.zbot ? e : g.zbot;
+    }
     return zt == 0 ? g.ztop : g.ztop + zt * TZ;
 }
 
@@ -127,7 +136,8 @@ struct StepArgs {
     Geom g;
     T h1, h2, h3;               // 1/dx, dx^2, 1/dx^2 (absorbingBoundaryCondition.c:159-161)
     T *u_next;                  // in: u_prev, out: u_next (in place, like the reference)
-    const T *psi_l, *psi_r, *psi_t, *psi_b;
+    const T *psi_l, *psi_r, *psi_t, *psi_b;   // psi of the previous step (read)
+    T *psn_l, *psn_r, *psn_t, *psn_b;         // psi of this step (written; the other buffer)
     T *xi_l, *xi_r, *xi_t, *xi_b;
     const float *a_l, *b_l, *a_r, *b_r, *a_t, *b_t, *a_b, *b_b;
     int t;                      // forward: time; backward: time (tau = nt-1-time)
@@ -151,6 +161,7 @@ struct StepArgs {
 // Tensor maps of one step: halo maps box {SZ, tx+8}, plain maps box {TZ, tx}.
 struct StepMaps {
     CUtensorMap cur;            // current propagated field (halo)
+    CUtensorMap cur8;           // ...with an 8-column x halo, box {SZ, tx+16} (side CPML tiles)
     CUtensorMap prev;           // previous propagated field = output buffer (plain)
     CUtensorMap coef;           // (v dt/dx)^2 (plain)
     CUtensorMap scur;           // backward reconstruction: current source field (halo)
@@ -198,17 +209,6 @@ struct BatchIndex {
     int nt[kMaxMembers];                // time steps of member i
 };
 
-template <typename T>
-struct PsiArgs {
-    Geom g;
-    T h1;
-    const T *u;                 // current wavefield
-    T *psi_l, *psi_r, *psi_t, *psi_b;
-    const float *a_l, *b_l, *a_r, *b_r, *a_t, *b_t, *a_b, *b_b;
-    T *ring;                    // forward, FP32 ring storage: u's ring cells go to this slot
-    int ring_only;              // save the ring only (after the last forward step)
-};
-
 // ---- batched steps (rtm_batch.cuh) -------------------------------------------------------
 // state[m] = (pass, step): pass 0 idle, 1 forward (nt steps), 2 backward (nt + 1 steps,
 // the last one images only), 3 finished.
@@ -237,10 +237,9 @@ template <typename T>
 cudaError_t launch_step(int backward, const StepMaps &maps, const StepArgs<T> &a, int grid,
                         int pdl, cudaStream_t s);
 template <typename T>
-cudaError_t launch_psi(const PsiArgs<T> &a, int pdl, cudaStream_t s);
-template <typename T>
 int step_grid(int backward, const Geom &g);      // persistent CTAs for one step
 size_t step_smem_bytes(int backward, int elem_size, int tx);
+constexpr int kMaxStripThickness = 120;   // top / bottom CPML: each band inside one z-tile
 template <typename T>
 cudaError_t launch_coef(const Geom &g, const float *vel, int vel_pitch, T *coef, float dx,
                         float dt, cudaStream_t s);

@@ -1,13 +1,11 @@
 // rtm_kernels.cu -- sm_103a kernels of the RTM engine.
 //
-//   k_step   one fused time step: 8th-order leapfrog (SRC/stencilDFM.c:7-31), CPML
-//            corrections (SRC/absorbingBoundaryCondition.c:191-357), source injection
+//   k_step   one fused time step: 8th-order leapfrog (SRC/stencilDFM.c:7-31), the CPML
+//            psi update and corrections (SRC/absorbingBoundaryCondition.c:150-361), source injection
 //            (SRC/forward_modeling.c:105-109) or receiver overwrite
 //            (SRC/backward_modeling.c:277-281), trace recording, boundary-ring or
 //            snapshot storage, reverse-time source reconstruction and the FP64
 //            cross-correlation image (SRC/image_conditions.c:20-33).
-//   k_psi    CPML psi update of the four strips (absorbingBoundaryCondition.c:171-189,
-//            219-235, 265-281, 312-328); runs before k_step each step.
 //   others   set-up (coef), seismogram transpose, image/field layout conversion, the
 //            post-stack Laplacian (SRC/math_functions.c:9-27).
 //
@@ -235,7 +233,15 @@ __device__ __forceinline__ float block_max(float v, float *red)
 
 #include "rtm_step.cuh"
 
-// ---- CPML psi update ----------------------------------------------------------------------
+// ---- CPML psi update of the batched members (k_bpsi) ----------------------------------------
+// dpsi of 4 cells from psi along a strided line: rows p[0..3] = f[-4..-1], p[4..7] = f[1..4].
+template <typename T>
+__device__ __forceinline__ T dpsi_x(const T (&m)[4][4], const T (&p)[4][4], int j)
+{
+    return (T)RTM_B4 * (p[3][j] - m[0][j]) + (T)RTM_B3 * (p[2][j] - m[1][j])
+         + (T)RTM_B2 * (p[1][j] - m[2][j]) + (T)RTM_B1 * (p[0][j] - m[3][j]);
+}
+
 // One 4-cell quad of a strip: psi_n = b psi_{n-1} + a D1(u_n) / dx, the reference's loops
 // absorbingBoundaryCondition.c:171-189 (left), 219-235 (top), 265-281 (right), 312-328
 // (bottom).  strip: 0 left, 1 top, 2 right, 3 bottom; idx: quad index within the strip;
@@ -317,69 +323,6 @@ __device__ __forceinline__ void psi_quad(const Geom &g, T h1, const T *u0, T *co
         if (z >= zlo && z < zhi) ps[j] = (T)bb[j] * ps[j] + (T)aa[j] * dpsi_z<T>(q, j) * h1;
     }
     st4(ps4, ps);
-}
-
-// Ring cells of psi quad (strip, idx) of k_psi's enumeration (psi_quad's decode), copied from
-// u to the ring slot: the side bands (corners included) by the left/right quads, the top and
-// bottom bands between them by the top/bottom quads -- every ring cell once.
-template <typename T>
-__device__ __forceinline__ void ring_save_quad(const Geom &g, const T *u, T *ring, int strip, int idx)
-{
-    int x, zq;
-    if (strip == 0 || strip == 2) {
-        const int th = strip == 0 ? g.thl : g.thr;
-        const int nq = (g.dimz - 8 + 3) / 4;
-        if (idx >= (th - 8) * nq) return;
-        const int li = 4 + idx / nq;
-        zq = 4 + 4 * (idx % nq);
-        x = strip == 0 ? li : g.dimx - g.thr + li;
-        if (x >= g.rx0 && x < g.rx1) return;
-    } else {
-        int nq, z0;
-        if (strip == 1) {
-            nq = (g.thu - 8 + 3) / 4;
-            z0 = 4;
-        } else {
-            z0 = (g.dimz - g.thd + 4) & ~3;
-            nq = (g.dimz - 4 - z0 + 3) / 4;
-        }
-        if (idx >= (g.dimx - 8) * nq) return;
-        x = 4 + idx / nq;
-        zq = z0 + 4 * (idx % nq);
-        if (x < g.rx0 || x >= g.rx1) return;
-    }
-    if (!ring_quad(g, x, zq)) return;
-    const T *col = u + (size_t)x * g.pitch;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int z = zq + j;
-        const int r = z < g.dimz ? ring_index(g, x, z) : -1;
-        if (r >= 0) ring[r] = col[z];
-    }
-}
-
-// Plain-plan psi kernel (the four strips' quads as one list).  With programmatic dependent
-// launch it first waits for the previous step kernel (whose output u_n it reads), then lets
-// the next step kernel start.  Forward with FP32 ring storage it also saves u_n's ring (slot n): done here,
-// on the strip quads, instead of inside the step kernel's boundary tiles (forward step 22.5 ->
-// 20.3 us on 3400 x 700).
-template <typename T>
-__global__ void __launch_bounds__(256) k_psi(const __grid_constant__ PsiArgs<T> a)
-{
-    griddep_wait();
-    griddep_launch();
-    int cnt[4];
-    psi_counts(a.g, cnt);
-    const int n = cnt[0] + cnt[1] + cnt[2] + cnt[3];
-    T *const psi[4] = {a.psi_l, a.psi_r, a.psi_t, a.psi_b};
-    const float *const prof[8] = {a.a_l, a.b_l, a.a_r, a.b_r, a.a_t, a.b_t, a.a_b, a.b_b};
-    // the four strips' quads as one list (left, top, right, bottom), grid-stride
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        int lq = q, strip = 0;
-        while (strip < 3 && lq >= cnt[strip]) lq -= cnt[strip++];
-        if (!a.ring_only) psi_quad<T>(a.g, a.h1, a.u, psi, prof, strip, lq, false);
-        if (a.ring) ring_save_quad<T>(a.g, a.u, a.ring, strip, lq);
-    }
 }
 
 #include "rtm_march.cuh"
@@ -591,8 +534,8 @@ int step_grid(int backward, const Geom &g)
 
 size_t step_smem_bytes(int backward, int elem_size, int tx)
 {
-    const size_t ut = (size_t)(tx + 2 * HALO) * SZ, pt = (size_t)tx * TZ;
-    const size_t stage = backward ? 2 * ut + 3 * pt : ut + 2 * pt;
+    const size_t ut8 = (size_t)(tx + 4 * HALO) * SZ, ut = (size_t)(tx + 2 * HALO) * SZ, pt = (size_t)tx * TZ;
+    const size_t stage = backward ? ut8 + ut + 3 * pt : ut8 + 2 * pt;
     const size_t ns = (elem_size == 4 && !backward) ? 3 : 2;
     return ns * stage * elem_size;
 }
@@ -615,35 +558,6 @@ cudaError_t launch_step(int backward, const StepMaps &maps, const StepArgs<T> &a
     if (warps == 16 && sizeof(T) == 4)
         return launch_step_w<T, 0, (sizeof(T) == 4 ? 16 : 8)>(maps, a, grid, pdl, s);
     return cudaErrorInvalidValue;
-}
-
-// psi CTAs per SM at most (grid-stride beyond): the step kernel that follows needs the SMs
-constexpr int kPsiCtasPerSm = 4;
-
-template <typename T>
-cudaError_t launch_psi(const PsiArgs<T> &a, int pdl, cudaStream_t s)
-{
-    int cnt[4];
-    psi_counts(a.g, cnt);
-    const int blocks = (cnt[0] + cnt[1] + cnt[2] + cnt[3] + 255) / 256;
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    const int cap = kPsiCtasPerSm * (sms > 0 ? sms : 1);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(blocks < cap ? blocks : cap);
-    cfg.blockDim = dim3(256);
-    cfg.stream = s;
-    cudaLaunchAttribute at = pdl_attr();
-    cfg.attrs = pdl ? &at : nullptr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    static cudaError_t carve = cudaFuncSetAttribute(k_psi<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                    cudaSharedmemCarveoutMaxShared);
-    if (carve != cudaSuccess) return carve;
-    return cudaLaunchKernelEx(&cfg, k_psi<T>, a);
 }
 
 template <typename T>
@@ -826,7 +740,6 @@ template int bstep_grid<float>();
     template cudaError_t launch_step<T>(int, const StepMaps &, const StepArgs<T> &, int, int,  \
                                         cudaStream_t);                                         \
     template int step_grid<T>(int, const Geom &);                                              \
-    template cudaError_t launch_psi<T>(const PsiArgs<T> &, int, cudaStream_t);                 \
     template cudaError_t launch_coef<T>(const Geom &, const float *, int, T *, float, float,   \
                                         cudaStream_t);                                         \
     template cudaError_t launch_image_out<T>(const Geom &, const double *, T *, int,           \

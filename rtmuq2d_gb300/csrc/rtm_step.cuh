@@ -1,26 +1,30 @@
 // rtm_step.cuh -- the persistent, TMA-pipelined time-step kernel k_step (included by
 // rtm_kernels.cu).
 //
-// Grid: a fixed number of CTAs (filling the SMs); CTA b processes tiles b, b+G, b+2G, ...
-// of the TX x 128 tiling (z-tile index fastest, so boundary and interior tiles interleave).
-// Each tile's inputs -- the current field with a 4-cell halo, u_prev and coef (backward
-// reconstruction: also the source field with halo and its predecessor) -- arrive by TMA 2-D
-// copies into one of NS shared-memory stages; thread 0 refills a stage as soon as its tile
-// is done, so NS-1 tiles are in flight while one is computed.
+// Grid: a fixed number of CTAs (filling the SMs); each CTA takes a static, balanced share of
+// the TX x 128 tiles of the step (boundary tiles first).  Each tile's inputs -- the current
+// field with a 4-cell halo (8 columns in x on the side CPML tiles), u_prev and coef
+// (backward reconstruction: also the source field with halo and its predecessor) -- arrive by
+// TMA 2-D copies into one of NS shared-memory stages; thread 0 refills a stage as soon as its
+// tile is done, so NS-1 tiles are in flight while one is computed.
 //
 // Per tile, every thread owns RXC = 2 columns x 4 consecutive z cells, keeps a 9-column
 // register window along x and reads z neighbours as aligned 16-byte vectors:
 //   * 8th-order leapfrog (SRC/stencilDFM.c:17-29);
-//   * on tiles touching the CPML, the corrections of the four strips in the reference's
-//     order left, top, right, bottom (SRC/absorbingBoundaryCondition.c:191-357), vectorised
-//     per 4-cell quad (psi and xi moved as 16-byte vectors);
+//   * on tiles touching the CPML, the whole CPML update of the step
+//     (SRC/absorbingBoundaryCondition.c:150-361): psi of the step computed in the tile from
+//     the halo of the current field (the reference's psi loops, :171-189, 219-235, 265-281,
+//     312-328), then the corrections of the four strips in the reference's order left, top,
+//     right, bottom (:191-357).  psi is double-buffered (read: the previous step's, written:
+//     this step's), so that a tile can rebuild the psi cells of its neighbours that its own
+//     corrections read while those neighbours write theirs;
 //   * source injection (SRC/forward_modeling.c:105-109) or receiver overwrite
 //     (backward_modeling.c:277-281), trace recording, boundary-ring or snapshot storage
 //     (FP32, or BF16/FP16 with a per-step, per-tile max-abs scale);
 //   * backward: reverse-time source reconstruction on the stencil-only region and the FP64
 //     cross-correlation image (SRC/image_conditions.c:20-33).
-// Chaining with k_psi uses programmatic dependent launch: psi is read only after
-// griddepcontrol.wait, and only by tiles that need it.
+// Consecutive steps chain by programmatic dependent launch: a step's CTAs start while the
+// previous step's last CTAs finish and issue their first tile loads after griddepcontrol.wait.
 
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" :::); }
@@ -28,9 +32,10 @@ __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.
 template <typename T, int WARPS, int BWD>
 struct StepCfg {
     static constexpr int TXC = WARPS * RXC;                       // x columns per tile
+    static constexpr int UT8 = (TXC + 4 * HALO) * SZ;             // current field, 8-column x halo
     static constexpr int UT = (TXC + 2 * HALO) * SZ;              // halo tile, elements
     static constexpr int PT = TXC * TZ;                           // plain tile, elements
-    static constexpr int STAGE = BWD ? 2 * UT + 3 * PT : UT + 2 * PT;
+    static constexpr int STAGE = BWD ? UT8 + UT + 3 * PT : UT8 + 2 * PT;
     static constexpr int NS = (sizeof(T) == 4 && !BWD) ? 3 : 2;   // pipeline stages
     static constexpr size_t SMEM = (size_t)NS * STAGE * sizeof(T);
 };
@@ -55,14 +60,16 @@ __device__ __forceinline__ void image_quad(double *img, double *slf, const T (&s
     reinterpret_cast<double2 *>(slf)[0] = s0; reinterpret_cast<double2 *>(slf)[1] = s1;
 }
 
-// dpsi of 4 cells from psi along a strided line: rows p[0..3] = f[-4..-1], p[4..7] = f[1..4].
+// First derivative (times dx) of 4 cells along x from a 9-column window W[k] = f(x-4+k):
+// B4 (f+4 - f-4) + B3 (f+3 - f-3) + B2 (f+2 - f-2) + B1 (f+1 - f-1), the operand order of
+// absorbingBoundaryCondition.c:177-181 (psi) and :198-203 (dpsi).
 template <typename T>
-__device__ __forceinline__ T dpsi_x(const T (&m)[4][4], const T (&p)[4][4], int j)
+__device__ __forceinline__ T d1x_w(const T (&W)[9][4], int j)
 {
-    return (T)RTM_B4 * (p[3][j] - m[0][j]) + (T)RTM_B3 * (p[2][j] - m[1][j])
-         + (T)RTM_B2 * (p[1][j] - m[2][j]) + (T)RTM_B1 * (p[0][j] - m[3][j]);
+    return (T)RTM_B4 * (W[8][j] - W[0][j]) + (T)RTM_B3 * (W[7][j] - W[1][j])
+         + (T)RTM_B2 * (W[6][j] - W[2][j]) + (T)RTM_B1 * (W[5][j] - W[3][j]);
 }
-// dpsi of 4 cells along z from a 12-value line q (q[4+j] is cell j).
+// The same along z from a 12-value line q (q[4+j] is cell j).
 template <typename T>
 __device__ __forceinline__ T dpsi_z(const T (&q)[12], int j)
 {
@@ -84,89 +91,6 @@ __device__ __forceinline__ T d2z_q(const T (&zz)[12], int j)
          + (T)RTM_AC0 * zz[4 + j];
 }
 
-// Left/right strip (x-derivative) correction of one quad.  psi, xi: strip arrays with row
-// stride P addressed at the quad; ab, bb: the column's profile values.
-template <typename T>
-__device__ __forceinline__ void cpml_x_quad(const T *psi, T *xi, size_t P, T ab, T bb, const T (&W)[9][4],
-                                            const T (&cf)[4], T (&v)[4], int zq, int zlo, int zhi,
-                                            T h1, T h2, T h3, bool fresh)
-{
-    // dpsi = B4 (f+4 - f-4) + B3 (f+3 - f-3) + B2 (f+2 - f-2) + B1 (f+1 - f-1), one row pair
-    // at a time (same operand order as absorbingBoundaryCondition.c:198-203)
-    T acc[4];
-    {
-        const T bk[4] = {(T)RTM_B4, (T)RTM_B3, (T)RTM_B2, (T)RTM_B1};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            T mk[4], pk[4];
-            ld4(psi - (ptrdiff_t)(4 - k) * (ptrdiff_t)P, mk);
-            ld4(psi + (ptrdiff_t)(4 - k) * (ptrdiff_t)P, pk);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const T term = bk[k] * (pk[j] - mk[j]);
-                acc[j] = k == 0 ? term : acc[j] + term;
-            }
-        }
-    }
-    T x4[4];
-    if (fresh) {                          // first step of a pass: xi starts from zero
-#pragma unroll
-        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
-    } else {
-        ld4(xi, x4);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int z = zq + j;
-        if (z >= zlo && z < zhi) {
-            const T dp = acc[j] * h1;
-            const T xn = bb * x4[j] + ab * (d2x_w<T>(W, j) * h3 + dp);
-            x4[j] = xn;
-            v[j] = v[j] + (cf[j] * h2) * (dp + xn);
-        }
-    }
-    st4(xi, x4);
-}
-
-// Top/bottom strip (z-derivative) correction of one quad.  psi, xi, ab, bb addressed at the
-// quad's first cell in 4-aligned strip arrays (psi readable at -4..+7).
-template <typename T>
-__device__ __forceinline__ void cpml_z_quad(const T *psi, T *xi, const float *ab, const float *bb,
-                                            const T (&zz)[12], const T (&cf)[4], T (&v)[4], int zq,
-                                            int zlo, int zhi, T h1, T h2, T h3, bool fresh)
-{
-    T q[12];
-    {
-        T a0[4], a1[4], a2[4];
-        ld4(psi - 4, a0);
-        ld4(psi, a1);
-        ld4(psi + 4, a2);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) { q[j] = a0[j]; q[4 + j] = a1[j]; q[8 + j] = a2[j]; }
-    }
-    T x4[4];
-    if (fresh) {                          // first step of a pass: xi starts from zero
-#pragma unroll
-        for (int j = 0; j < 4; ++j) x4[j] = (T)0;
-    } else {
-        ld4(xi, x4);
-    }
-    const float4 av = *reinterpret_cast<const float4 *>(ab);
-    const float4 bv = *reinterpret_cast<const float4 *>(bb);
-    const float aa[4] = {av.x, av.y, av.z, av.w}, bbv[4] = {bv.x, bv.y, bv.z, bv.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int z = zq + j;
-        if (z >= zlo && z < zhi) {
-            const T dp = dpsi_z<T>(q, j) * h1;
-            const T xn = (T)bbv[j] * x4[j] + (T)aa[j] * (d2z_q<T>(zz, j) * h3 + dp);
-            x4[j] = xn;
-            v[j] = v[j] + (cf[j] * h2) * (dp + xn);
-        }
-    }
-    st4(xi, x4);
-}
-
 // Loads the 12-value z line (zm | centre | zp) of column row `row` of a halo tile.
 template <typename T>
 __device__ __forceinline__ void z_line(const T *tile, int row, int zi, const T (&c)[4], T (&zz)[12])
@@ -178,95 +102,301 @@ __device__ __forceinline__ void z_line(const T *tile, int row, int zi, const T (
     for (int j = 0; j < 4; ++j) { zz[j] = zm[j]; zz[4 + j] = c[j]; zz[8 + j] = zp[j]; }
 }
 
-// All CPML corrections of one quad (column c, quad qi) of a boundary tile, in the
-// reference's strip order left, top, right, bottom, on the stencil result in O.
+// The x-strip (left or right) whose psi array holds column x, if any: the left array covers
+// [0, th_left), the right one [dimX-th_right, dimX).  Sets the column's arrays (old psi, new
+// psi, xi; row stride pitch) and profile values; *upd: x is one of the strip's psi /
+// correction columns, [4, th_left-4) or [dimX-th_right+4, dimX-4)
+// (absorbingBoundaryCondition.c:174, 266).  The other columns of an array keep their psi,
+// which the corrections next to them read.
 template <typename T>
-__device__ __forceinline__ void cpml_quad_all(const StepArgs<T> &a, const T *su, const T *scf, T *O,
-                                              int x0, int z0, int c, int qi)
+__device__ __forceinline__ bool x_strip(const StepArgs<T> &a, int x, const T *&po, T *&pn, T *&xi, T &ab,
+                                        T &bb, bool &upd)
 {
     const Geom &g = a.g;
     const size_t P = (size_t)g.pitch;
-    const int x = x0 + c, zq = z0 + 4 * qi;
-    const bool zx = zq + 4 > 4 && zq < g.dimz - 4;              // quad meets [4, dimZ-4)
-    const bool inL = zx && x >= 4 && x < g.thl - 4;
-    const bool inR = zx && x >= g.dimx - g.thr + 4 && x < g.dimx - 4;
-    const bool inT = zq + 4 > 4 && zq < g.thu - 4;               // every column (the quirk)
-    const bool inB = x >= 4 && x < g.dimx - 4 && zq + 4 > g.dimz - g.thd + 4 && zq < g.dimz - 4;
-    if (!(inL || inR || inT || inB)) return;
-    const bool fresh = (a.flags & F_STRIPS_FRESH) != 0;
-    T v[4], cf[4];
-    ld4(O + c * TZ + 4 * qi, v);
-    ld4(scf + c * TZ + 4 * qi, cf);
-    const T *col = su + (c + HALO) * SZ + 4 * qi + HALO;         // centre quad in the halo tile
-    if (inL || inR) {
-        T W[9][4];
-#pragma unroll
-        for (int m = 0; m < 9; ++m) ld4(col + (m - 4) * SZ, W[m]);
-        if (inL)
-            cpml_x_quad<T>(a.psi_l + (size_t)x * P + zq, a.xi_l + (size_t)x * P + zq, P, (T)a.a_l[x],
-                           (T)a.b_l[x], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
-        if (inT) {
-            T zz[12];
-            z_line<T>(su, c + HALO, 4 * qi + HALO, W[4], zz);
-            cpml_z_quad<T>(a.psi_t + (size_t)x * g.st + zq, a.xi_t + (size_t)x * g.st + zq, a.a_t + zq,
-                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3, fresh);
-        }
-        if (inR) {
-            const int li = x - (g.dimx - g.thr);
-            cpml_x_quad<T>(a.psi_r + (size_t)li * P + zq, a.xi_r + (size_t)li * P + zq, P, (T)a.a_r[li],
-                           (T)a.b_r[li], W, cf, v, zq, 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
-        }
-        if (inB) {
-            T zz[12];
-            z_line<T>(su, c + HALO, 4 * qi + HALO, W[4], zz);
-            const int lq = zq - g.zb0;
-            cpml_z_quad<T>(a.psi_b + (size_t)x * g.sb + lq, a.xi_b + (size_t)x * g.sb + lq, a.a_b + lq,
-                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
-        }
-    } else {
-        T c4[4], zz[12];
-        ld4(col, c4);
-        z_line<T>(su, c + HALO, 4 * qi + HALO, c4, zz);
-        if (inT)
-            cpml_z_quad<T>(a.psi_t + (size_t)x * g.st + zq, a.xi_t + (size_t)x * g.st + zq, a.a_t + zq,
-                           a.b_t + zq, zz, cf, v, zq, 4, g.thu - 4, a.h1, a.h2, a.h3, fresh);
-        if (inB) {
-            const int lq = zq - g.zb0;
-            cpml_z_quad<T>(a.psi_b + (size_t)x * g.sb + lq, a.xi_b + (size_t)x * g.sb + lq, a.a_b + lq,
-                           a.b_b + lq, zz, cf, v, zq, g.dimz - g.thd + 4, g.dimz - 4, a.h1, a.h2, a.h3, fresh);
-        }
+    if (x >= 0 && x < g.thl) {
+        po = a.psi_l + (size_t)x * P; pn = a.psn_l + (size_t)x * P; xi = a.xi_l + (size_t)x * P;
+        ab = (T)a.a_l[x]; bb = (T)a.b_l[x];
+        upd = x >= 4 && x < g.thl - 4;
+        return true;
     }
-    st4(O + c * TZ + 4 * qi, v);
+    if (x >= g.dimx - g.thr && x < g.dimx) {
+        const int li = x - (g.dimx - g.thr);
+        po = a.psi_r + (size_t)li * P; pn = a.psn_r + (size_t)li * P; xi = a.xi_r + (size_t)li * P;
+        ab = (T)a.a_r[li]; bb = (T)a.b_r[li];
+        upd = li >= 4 && x < g.dimx - 4;
+        return true;
+    }
+    return false;
 }
 
-// One pass over every quad of a boundary tile (threads take quads from a compact list).
-template <typename T, int TXC>
-__device__ __forceinline__ void cpml_pass(const StepArgs<T> &a, const T *su, const T *scf, T *O,
-                                          int x0, int z0, int z1)
+// psi of this step on 4 cells of an x-strip column from the 9-column window of u and the
+// previous psi (absorbingBoundaryCondition.c:177-181, 269-273): psi = b psi + a D1x(u) / dx on
+// z in [4, dimZ-4); the other cells keep their psi.
+template <typename T>
+__device__ __forceinline__ void psi_x_new(const T (&W)[9][4], T (&ps)[4], T ab, T bb, T h1, int zq, int dimz)
 {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (zq + j >= 4 && zq + j < dimz - 4) ps[j] = bb * ps[j] + ab * d1x_w<T>(W, j) * h1;
+}
+
+// The CPML update of a tile touching a strip, on the stencil results v of the thread's own
+// cells (RXC columns x one 4-cell quad), in registers.  Per strip cell, in the reference's
+// order left, top, right, bottom: dpsi = D1(psi)/dx, xi = b xi + a (D2(u)/dx^2 + dpsi),
+// u_next += coef dx^2 (dpsi + xi) (absorbingBoundaryCondition.c:191-217, 237-263, 283-310,
+// 330-357), with the psi of this step computed here:
+//   * x-strips (left, right; only the side tiles): a thread computes the psi of its own cells
+//     (from the 9-column window of u) into the stage's u_prev tile, which only it has read;
+//     the tile computes the psi of the 4 columns on either side (from the 8-column halo) into
+//     the u rows of the outermost halo columns, which nothing reads after that; the
+//     corrections read both;
+//   * z-strips (top, bottom): every tile row holds a whole band plus 4 rows, so a lane
+//     computes the psi of its own quad from the tile's z line and takes its neighbours' from
+//     the lanes above and below (warp shuffles).
+// u8: the stage's current-field area (tile column c at row c + 8; 4-halo tiles fill rows
+// 4 .. TXC + 12); sprv: the stage's u_prev tile.  The previous psi, xi and the profiles come
+// from global memory, each thread's loads issued before the work that needs them.
+template <typename T, int WARPS>
+__device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv, const T *scf, T (&v)[RXC][4],
+                                           int x0, int z0, int z1)
+{
+    constexpr int TXC = WARPS * RXC;
+    constexpr int NTHR = WARPS * 32;
+    constexpr int RING_ITEMS = 8 * 32;                      // 4 columns either side x 32 quads
+    constexpr int RPT = (RING_ITEMS + NTHR - 1) / NTHR;    // ring items per thread
     const Geom &g = a.g;
-    const int ncol = min(TXC, g.dimx - x0);
-    const int nq = (min(z1, g.dimz) - z0 + 3) >> 2;
-    const int n = ncol * nq;
-    for (int item = threadIdx.x; item < n; item += blockDim.x)
-        cpml_quad_all<T>(a, su, scf, O, x0, z0, item / nq, item % nq);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int zq = z0 + 4 * lane;
+    const int zi = 4 * lane + HALO;                 // the quad's first cell within a halo column
+    const T *su = u8 + HALO * SZ;                   // 4-halo view: tile column c at row c + HALO
+    const int zend = min(z1, g.dimz);
+    const bool own = zq < zend;                     // the quad belongs to this tile
+    const bool qT = zq + 4 > 4 && zq < g.thu - 4;                        // top correction rows
+    const bool qB = zq + 4 > g.dimz - g.thd + 4 && zq < g.dimz - 4;      // bottom ones
+    const bool tX = x0 < g.thl - 4 || x0 + TXC > g.dimx - g.thr + 4;     // tile-uniform
+    const bool tZ = z0 < g.thu - 4 || zend > g.dimz - g.thd + 4;
+    // the quad in the top psi array (rows [0, th_up)) or the bottom one (rows [zb0, dimZ))
+    const bool inTa = own && zq < g.thu;
+    const bool inBa = own && !inTa && zq >= g.zb0;
+    const T h1 = a.h1, h2 = a.h2, h3 = a.h3;
+
+    // ---- z-strip loads (previous psi, xi) of both columns, issued first
+    T psZ[RXC][4], xZ[RXC][4];
+#pragma unroll
+    for (int r = 0; r < RXC; ++r) {
+        const int x = x0 + warp * RXC + r;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { psZ[r][j] = (T)0; xZ[r][j] = (T)0; }
+        if (tZ && (inTa || inBa) && x < g.dimx) {
+            const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
+            ld4((inTa ? a.psi_t : a.psi_b) + o, psZ[r]);
+            if (qT || qB) ld4((inTa ? a.xi_t : a.xi_b) + o, xZ[r]);
+        }
+    }
+
+    // ---- x-strips
+    T dX[RXC][4];
+    bool cX[RXC];
+#pragma unroll
+    for (int r = 0; r < RXC; ++r) {
+        cX[r] = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dX[r][j] = (T)0;
+    }
+    if (tX) {
+        const bool zin = zq + 4 > 4 && zq < g.dimz - 4;
+        T xX[RXC][4];
+        // psi of the 4 columns either side (read the whole 8-column halo)
+        T psR[RPT][4];
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int item = threadIdx.x + k * NTHR;
+            const int rc = item >> 5, l = item & 31;
+            const int c = rc < 4 ? rc - 4 : TXC + rc - 4;
+            const int zr = z0 + 4 * l;
+            const T *po; T *pn, *xi; T ab, bb;
+            bool upd = false, arr = false;
+            if (item < RING_ITEMS && zr < zend) arr = x_strip<T>(a, x0 + c, po, pn, xi, ab, bb, upd);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) psR[k][j] = (T)0;
+            if (arr) {
+                ld4(po + zr, psR[k]);
+                if (upd && zr + 4 > 4 && zr < g.dimz - 4) {
+                    T W[9][4];
+#pragma unroll
+                    for (int m = 0; m < 9; ++m) ld4(u8 + (c + 4 + m) * SZ + 4 * l + HALO, W[m]);
+                    psi_x_new<T>(W, psR[k], ab, bb, h1, zr, g.dimz);
+                }
+            }
+        }
+        // psi of the own cells, into the u_prev tile (each thread overwrites only what it read)
+#pragma unroll
+        for (int r = 0; r < RXC; ++r) {
+            const int c = warp * RXC + r, x = x0 + c;
+            T ps[4] = {(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) xX[r][j] = (T)0;
+            const T *po; T *pn, *xi; T ab, bb;
+            bool upd;
+            if (own && x_strip<T>(a, x, po, pn, xi, ab, bb, upd)) {
+                ld4(po + zq, ps);
+                if (upd && zin) {
+                    cX[r] = true;
+                    ld4(xi + zq, xX[r]);
+                    T W[9][4];
+#pragma unroll
+                    for (int m = 0; m < 9; ++m) ld4(su + (c + m) * SZ + zi, W[m]);
+                    psi_x_new<T>(W, ps, ab, bb, h1, zq, g.dimz);
+                }
+                st4(pn + zq, ps);
+            }
+            st4(sprv + c * TZ + 4 * lane, ps);
+        }
+        __syncthreads();                              // the outermost halo columns are read
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int item = threadIdx.x + k * NTHR;
+            if (item < RING_ITEMS) {
+                const int rc = item >> 5, l = item & 31;
+                st4(u8 + (rc < 4 ? rc : TXC + 8 + rc) * SZ + 4 * l, psR[k]);
+            }
+        }
+        __syncthreads();
+        // psi of tile column cc (-4 <= cc < TXC + 4) at this thread's quad
+        auto psi_at = [&](int cc, T (&out)[4]) {
+            if (cc < 0) ld4(u8 + (cc + 4) * SZ + 4 * lane, out);
+            else if (cc >= TXC) ld4(u8 + (cc + 12) * SZ + 4 * lane, out);
+            else ld4(sprv + cc * TZ + 4 * lane, out);
+        };
+#pragma unroll
+        for (int r = 0; r < RXC; ++r) {
+            if (!cX[r]) continue;
+            const int c = warp * RXC + r, x = x0 + c;
+            const T *po; T *pn, *xi; T ab, bb;
+            bool upd;
+            x_strip<T>(a, x, po, pn, xi, ab, bb, upd);
+            const T bk[4] = {(T)RTM_B4, (T)RTM_B3, (T)RTM_B2, (T)RTM_B1};
+            T acc[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                T mk[4], pk[4];
+                psi_at(c - (4 - k), mk);
+                psi_at(c + (4 - k), pk);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const T term = bk[k] * (pk[j] - mk[j]);
+                    acc[j] = k == 0 ? term : acc[j] + term;
+                }
+            }
+            T W[9][4], cf[4];
+#pragma unroll
+            for (int m = 0; m < 9; ++m) ld4(su + (c + m) * SZ + zi, W[m]);
+            ld4(scf + c * TZ + 4 * lane, cf);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int z = zq + j;
+                if (z >= 4 && z < g.dimz - 4) {
+                    const T dp = acc[j] * h1;
+                    const T xn = bb * xX[r][j] + ab * (d2x_w<T>(W, j) * h3 + dp);
+                    xX[r][j] = xn;
+                    dX[r][j] = (cf[j] * h2) * (dp + xn);
+                }
+            }
+            st4(xi + zq, xX[r]);
+        }
+    }
+
+    // ---- z-strips: psi of the own quad (absorbingBoundaryCondition.c:225-229, 318-322), the
+    // neighbours' by shuffle, the correction term; the corrections applied in strip order
+    float aa[4] = {0.f, 0.f, 0.f, 0.f}, bz[4] = {0.f, 0.f, 0.f, 0.f};
+    const int zlo = inTa ? 4 : g.dimz - g.thd + 4, zhi = inTa ? g.thu - 4 : g.dimz - 4;
+    if (tZ && (inTa || inBa)) {
+        const float *pa = inTa ? a.a_t + zq : a.a_b + (zq - g.zb0);
+        const float *pb = inTa ? a.b_t + zq : a.b_b + (zq - g.zb0);
+        const float4 av = *reinterpret_cast<const float4 *>(pa);
+        const float4 bv = *reinterpret_cast<const float4 *>(pb);
+        aa[0] = av.x; aa[1] = av.y; aa[2] = av.z; aa[3] = av.w;
+        bz[0] = bv.x; bz[1] = bv.y; bz[2] = bv.z; bz[3] = bv.w;
+    }
+#pragma unroll
+    for (int r = 0; r < RXC; ++r) {
+        const int c = warp * RXC + r, x = x0 + c;
+        const bool left = cX[r] && x < g.thl;
+        T dZ[4] = {(T)0, (T)0, (T)0, (T)0};
+        bool cZ = false;
+        if (tZ) {
+            const bool arr = (inTa || inBa) && x < g.dimx;
+            cZ = arr && (qT || (qB && x >= 4 && x < g.dimx - 4));   // the top rows cover every column
+            T zz[12];
+            {
+                T c4[4];
+                ld4(su + (c + HALO) * SZ + zi, c4);
+                z_line<T>(su, c + HALO, zi, c4, zz);
+            }
+            if (arr) {
+                if (x >= 4 && x < g.dimx - 4) {       // psi cells: x in [4, dimX-4)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int z = zq + j;
+                        if (z >= zlo && z < zhi)
+                            psZ[r][j] = (T)bz[j] * psZ[r][j] + (T)aa[j] * dpsi_z<T>(zz, j) * h1;
+                    }
+                }
+                const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
+                st4((inTa ? a.psn_t : a.psn_b) + o, psZ[r]);
+            }
+            T q[12];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const T up = __shfl_up_sync(0xffffffffu, psZ[r][j], 1);
+                const T dn = __shfl_down_sync(0xffffffffu, psZ[r][j], 1);
+                q[j] = lane > 0 ? up : (T)0;
+                q[4 + j] = psZ[r][j];
+                q[8 + j] = lane < 31 ? dn : (T)0;
+            }
+            if (cZ) {
+                T cf[4];
+                ld4(scf + c * TZ + 4 * lane, cf);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int z = zq + j;
+                    if (z >= zlo && z < zhi) {
+                        const T dp = dpsi_z<T>(q, j) * h1;
+                        const T xn = (T)bz[j] * xZ[r][j] + (T)aa[j] * (d2z_q<T>(zz, j) * h3 + dp);
+                        xZ[r][j] = xn;
+                        dZ[j] = (cf[j] * h2) * (dp + xn);
+                    }
+                }
+                const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
+                st4((inTa ? a.xi_t : a.xi_b) + o, xZ[r]);
+            }
+        }
+        // order: left, top, right, bottom
+        const bool xfirst = cX[r] && (left || !qT);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (xfirst) v[r][j] = v[r][j] + dX[r][j];
+            if (cZ) v[r][j] = v[r][j] + dZ[j];
+            if (cX[r] && !xfirst) v[r][j] = v[r][j] + dX[r][j];
+        }
+    }
 }
 
 template <typename T, int BWD, int WARPS>
-__device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, int t, bool &psi_ready,
-                                          float *red)
+__device__ __forceinline__ void step_tile(const StepArgs<T> &a, T *stage, int t, float *red)
 {
     using Cfg = StepCfg<T, WARPS, BWD>;
-    constexpr int TXC = Cfg::TXC, UT = Cfg::UT, PT = Cfg::PT;
+    constexpr int TXC = Cfg::TXC, UT8 = Cfg::UT8, UT = Cfg::UT, PT = Cfg::PT;
     const Geom &g = a.g;
     const int flags = a.flags;
     const bool recon = BWD && (flags & F_RECON);
-    const T *su = stage;                 // current field + halo   [TXC+8][SZ]
-    T *sprv = const_cast<T *>(stage) + UT;   // previous field [TXC][TZ]; boundary tiles reuse
-                                             // it as the output tile once it has been read
-    const T *scf = stage + UT + PT;      // coef                    [TXC][TZ]
-    const T *ss = stage + UT + 2 * PT;   // source field + halo     (backward reconstruction)
-    const T *ssp = stage + 2 * UT + 2 * PT;
+    T *su8 = stage;                      // current field, 8-column x halo area [TXC+16][SZ]
+    const T *su = stage + HALO * SZ;     // ...its 4-halo view               [TXC+8][SZ]
+    const T *sprv = stage + UT8;         // previous field                    [TXC][TZ]
+    const T *scf = stage + UT8 + PT;     // coef                              [TXC][TZ]
+    const T *ss = stage + UT8 + 2 * PT;  // source field + halo   (backward reconstruction)
+    const T *ssp = stage + UT8 + UT + 2 * PT;
 
     int xt, zt;
     tile_coords(g, t, xt, zt);
@@ -338,20 +468,8 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, const T *stage, 
     }
 
     if (boundary) {
-        // ---- CPML: stencil results to the output tile, four compact strip passes
-        if (cpml_t) {
-            if (!psi_ready) {            // psi of this step comes from the preceding k_psi
-                griddep_wait();
-                psi_ready = true;
-            }
-#pragma unroll
-            for (int r = 0; r < RXC; ++r) st4(sprv + (row0 + r) * TZ + 4 * lane, v[r]);
-            __syncthreads();
-            cpml_pass<T, TXC>(a, su, scf, sprv, x0, z0, z1);
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < RXC; ++r) ld4(sprv + (row0 + r) * TZ + 4 * lane, v[r]);
-        }
+        // ---- CPML: psi of this step and the four strips' corrections, on v in registers
+        if (cpml_t) cpml_fused<T, WARPS>(a, su8, const_cast<T *>(sprv), scf, v, x0, z0, z1);
         // ---- the thread's own cells: source, receivers, stores, storage
         float mx = 0.0f;
 #pragma unroll
@@ -512,7 +630,7 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
     k_step(const __grid_constant__ StepMaps m, const __grid_constant__ StepArgs<T> a)
 {
     using Cfg = StepCfg<T, WARPS, BWD>;
-    constexpr int UT = Cfg::UT, PT = Cfg::PT, STAGE = Cfg::STAGE, NS = Cfg::NS, TXC = Cfg::TXC;
+    constexpr int UT8 = Cfg::UT8, UT = Cfg::UT, PT = Cfg::PT, STAGE = Cfg::STAGE, NS = Cfg::NS, TXC = Cfg::TXC;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T *stage0 = reinterpret_cast<T *>(smem_raw);
     __shared__ __align__(8) uint64_t full[NS];
@@ -520,7 +638,11 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
     __shared__ float red[WARPS];
     const Geom &g = a.g;
     const bool recon = BWD && (a.flags & F_RECON);
-    const uint32_t tile_bytes = (uint32_t)(sizeof(T) * (recon ? 2 * UT + 3 * PT : UT + 2 * PT));
+    const bool cpml_on = !(a.flags & F_NO_CPML);
+    // bytes of one tile's loads; the side CPML tiles load the current field with 8 halo
+    // columns on either side (their psi needs D1x(u) 4 columns beyond the tile)
+    const uint32_t tile_bytes = (uint32_t)(sizeof(T) * (recon ? UT + UT + 3 * PT : UT + 2 * PT));
+    const uint32_t side_bytes = tile_bytes + (uint32_t)(sizeof(T) * (UT8 - UT));
 
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -570,23 +692,27 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
         int xt, zt;
         tile_coords(g, t, xt, zt);
         const int x0 = xt * TXC, z0 = ztile_origin(g, zt);
+        const bool side = cpml_on && (x0 < g.thl - 4 || x0 + TXC > g.dimx - g.thr + 4);
         T *st = stage0 + (size_t)s * STAGE;
-        mbar_arrive_expect_tx(&full[s], tile_bytes);
-        tma_load_2d(st, &m.cur, z0 - HALO, x0 - HALO, &full[s]);
-        tma_load_2d(st + UT, &m.prev, z0, x0, &full[s]);
-        tma_load_2d(st + UT + PT, &m.coef, z0, x0, &full[s]);
+        mbar_arrive_expect_tx(&full[s], side ? side_bytes : tile_bytes);
+        if (side) tma_load_2d(st, &m.cur8, z0 - HALO, x0 - 2 * HALO, &full[s]);
+        else tma_load_2d(st + HALO * SZ, &m.cur, z0 - HALO, x0 - HALO, &full[s]);
+        tma_load_2d(st + UT8, &m.prev, z0, x0, &full[s]);
+        tma_load_2d(st + UT8 + PT, &m.coef, z0, x0, &full[s]);
         if (recon) {
-            tma_load_2d(st + UT + 2 * PT, &m.scur, z0 - HALO, x0 - HALO, &full[s]);
-            tma_load_2d(st + 2 * UT + 2 * PT, &m.sprev, z0, x0, &full[s]);
+            tma_load_2d(st + UT8 + 2 * PT, &m.scur, z0 - HALO, x0 - HALO, &full[s]);
+            tma_load_2d(st + UT8 + UT + 2 * PT, &m.sprev, z0, x0, &full[s]);
         }
     };
     if (threadIdx.x == 0) {
+        // the previous step (same stream, programmatic dependent launch) wrote this step's
+        // inputs: wait for its completion before the first load
+        griddep_wait();
         for (int s = 0; s < NS; ++s) issue(s, s);
     }
     // The next kernel in the stream may be scheduled now; it waits for this grid's
     // completion (griddepcontrol.wait) before it touches anything this grid writes.
     griddep_launch();
-    bool psi_ready = false;
     for (int i = 0;; ++i) {
         const int s = i % NS;
         const uint32_t par = (uint32_t)((i / NS) & 1);
@@ -604,7 +730,7 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
         }
         const int t = *reinterpret_cast<volatile int *>(&tile_of[s]);
         if (t >= g.tiles) break;                 // tiles are consumed in issue order
-        step_tile<T, BWD, WARPS>(a, stage0 + (size_t)s * STAGE, t, psi_ready, red);
+        step_tile<T, BWD, WARPS>(a, stage0 + (size_t)s * STAGE, t, red);
         __syncthreads();                         // stage s is free again
         if (threadIdx.x == 0) issue(i + NS, s);
     }
