@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--serve-load-high", type=float, default=1.5,
                     help="second pass of the same trace at this load: a standing queue, the "
                          "server full (0: skip)")
+    ap.add_argument("--plain-trace-requests", type=int, default=48,
+                    help="serving trace: requests also served one at a time by the plain path")
+    ap.add_argument("--plain-trace-seconds", type=float, default=25.0,
+                    help="serving trace: wall-time bound of the plain path's run")
     ap.add_argument("--serve-capacity", type=float, default=150.0,
                     help="with --only served: the batched capacity (Gcell-updates/s) the arrival "
                          "rate is sized by")
@@ -145,14 +149,16 @@ METRIC = "RTM Gcell-updates/s + p50/p99 migration latency: served vs plain, rel-
 def algorithmic_bytes(p):
     """Algorithmic DRAM bytes per launch of each kernel (FP32 fields, ring storage).
     k_step forward : 16 B per cell (u_cur, u_prev, coef read; u_next write)
-                     + 12 B per CPML-correction cell (psi read, xi read+write)
+                     + 16 B per CPML-correction cell (previous psi read, new psi write, xi
+                       read + write: the step kernel updates psi itself)
                      + 4 B per ring cell written
-    k_step backward: receiver field as forward (16 B/cell + 12 B/CPML cell)
+    k_step backward: receiver field as forward (16 B/cell + 16 B/CPML cell)
                      + 12 B per reconstruction-region cell (S_cur, S_prev read; S_next write)
                      + 4 B per ring cell read + 4 B per receiver (seismogram row)
                      + imaging every time_slices steps: 32 B per interior cell (FP64
                        image and self image read+write), averaged per launch
-    k_psi          : 12 B per psi cell (u read, psi read+write)."""
+    k_psi          : 12 B per psi cell (u read, psi read+write): the batched members' psi
+                     kernel (k_bpsi)."""
     dx, dz = p.dim_x, p.dim_z
     cells = dx * dz
     thl, thr, thu, thd = p.th_left, p.th_right, p.th_up, p.th_down
@@ -161,9 +167,10 @@ def algorithmic_bytes(p):
     ring = 8 * (p.nx + 16) + 8 * (p.nz + 8)
     region = (p.nx + 8) * (p.nz + 8)
     interior = p.nx * p.nz
-    fwd = 16 * cells + 12 * corr + 4 * ring
-    bwd = 16 * cells + 12 * corr + 12 * region + 4 * ring + 4 * p.rec_count + 32 * interior / p.time_slices
-    return {"k_step_fwd": fwd, "k_step_bwd": bwd, "k_psi": 12 * psi}
+    fwd = 16 * cells + 16 * corr + 4 * ring
+    bwd = 16 * cells + 16 * corr + 12 * region + 4 * ring + 4 * p.rec_count + 32 * interior / p.time_slices
+    batched_fwd = 16 * cells + 12 * corr + 4 * ring + 12 * psi   # k_mstep + k_bpsi + k_bstrip
+    return {"k_step_fwd": fwd, "k_step_bwd": bwd, "k_psi": 12 * psi, "batched_fwd_step": batched_fwd}
 
 
 def hbm_peak():
@@ -325,6 +332,7 @@ def summary(line):
         return round(x, 4) if isinstance(x, float) else x
 
     out = {"plain": {"value": r3(line["value"]), "e2e": r3(line["e2e"]["value"]),
+                     "e2e_zfp": r3(line["e2e_zfp"]["value"]) if line.get("e2e_zfp") else None,
                      "roofline_frac": r3(line["roofline"]["frac"])}}
     b = line.get("batched")
     if b:
@@ -338,9 +346,11 @@ def summary(line):
     if s:
         out["served"] = {k: r3(v) for k, v in pick(s, "requests", "value", "p50_latency_s", "p99_latency_s",
                                                    "hbm_occupancy_mean", "speedup_vs_plain_same_requests").items()}
-        if s.get("plain"):
-            out["served"]["plain_p50_s"] = r3(s["plain"].get("p50_latency_s"))
-            out["served"]["plain_p99_s"] = r3(s["plain"].get("p99_latency_s"))
+        if s.get("plain") and s.get("served_same_requests"):
+            out["served"]["same_requests"] = s["plain"]["requests"]
+            out["served"]["served_p50_p99_s"] = [r3(s["served_same_requests"]["p50_latency_s"]),
+                                                 r3(s["served_same_requests"]["p99_latency_s"])]
+            out["served"]["plain_p50_p99_s"] = [r3(s["plain"]["p50_latency_s"]), r3(s["plain"]["p99_latency_s"])]
     par = line.get("parity")
     if par:
         out["parity"] = {k: (float("%.3g" % v) if isinstance(v, float) else v) for k, v in par.items()
@@ -407,7 +417,7 @@ def run_batched(args, eng, rank=0, ws=1):
     srv.close()
     step_roof = None
     if fwd_steps:
-        step_bytes = sum(algorithmic_bytes(p)["k_step_fwd"] + algorithmic_bytes(p)["k_psi"] for p, *_ in inputs)
+        step_bytes = sum(algorithmic_bytes(p)["batched_fwd_step"] for p, *_ in inputs)
         achieved = step_bytes / (fwd_ms / fwd_steps * 1e-3) / 1e9
         peak, peak_kind = hbm_peak()
         step_roof = {"bound": "hbm", "what": "whole batched forward step (k_mstep + k_bpsi + k_bstrip)",
@@ -517,7 +527,7 @@ def serve_trace(args, eng, prepared, tol, capacity_gcells, load):
     srv.close()
     lat = np.array([done[k] - (t_start + arrivals[k]) for k in range(len(prepared))])
     cells = sum(p.cell_updates for p, *_ in prepared)
-    return {"value": cells / wall / 1e9, "unit": "Gcell-updates/s",
+    return {"_latencies": lat, "_arrivals": arrivals, "value": cells / wall / 1e9, "unit": "Gcell-updates/s",
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "mean_latency_s": float(lat.mean()), "seconds": wall,
             "arrival_rate_per_s": rate, "offered_load": load,
@@ -552,6 +562,44 @@ def plain_on_requests(eng, prepared, tol, n_sample=8):
     return sum(p.cell_updates for p, *_ in jobs) / dt / 1e9, len(jobs)
 
 
+def plain_trace(eng, prepared, tol, arrivals, k_max, seconds):
+    """The plain path serving the same arrivals: the first requests of the trace (at most
+    k_max, stopping after `seconds` of wall time) at their Poisson arrival times, one at a time
+    in arrival order through rtm_migrate_shot_zfp (the ZFP seismogram decoded on a host thread
+    while the forward pass runs).  Latency = completion - arrival, as for the served requests; the
+    service time (decode + migration) of each request is reported beside it.  Each grid's plan
+    is warmed by one untimed call first."""
+    seen = set()
+    for p, ext, wav, stream in prepared[:k_max]:
+        key = (p.nx, p.nz, p.nt, p.precision)
+        if key not in seen:
+            seen.add(key)
+            eng.migrate_shot(p, ext, wav, eng.zfp_decode(stream, p.rec_count, p.nt, tol))
+    lat, service, cells = [], [], 0
+    t_start = time.monotonic()
+    for k, (p, ext, wav, stream) in enumerate(prepared[:k_max]):
+        now = time.monotonic() - t_start
+        if now > seconds:
+            break
+        if arrivals[k] > now:
+            time.sleep(arrivals[k] - now)
+        t0 = time.monotonic()
+        eng.migrate_shot_zfp(p, ext, wav, stream, tol)
+        t1 = time.monotonic()
+        lat.append(t1 - (t_start + arrivals[k]))
+        service.append(t1 - t0)
+        cells += p.cell_updates
+    wall = time.monotonic() - t_start
+    eng.release_cached()
+    lat, service = np.array(lat), np.array(service)
+    return {"requests": int(len(lat)), "value": cells / wall / 1e9, "unit": "Gcell-updates/s",
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "service_p50_s": float(np.percentile(service, 50)),
+            "service_p99_s": float(np.percentile(service, 99)),
+            "note": "the first requests of the same trace at the same arrival times, served one at a "
+                    "time (rtm_migrate_shot_zfp each); latency includes the queueing"}
+
+
 def run_served(args, eng, capacity_gcells):
     """The serving trace at `serve_load` x the batched capacity (the latency view), and the
     same trace at `serve_load_high` (a standing queue: the server's throughput when full);
@@ -559,13 +607,24 @@ def run_served(args, eng, capacity_gcells):
     from rtmuq2d_gb300 import workloads
     prepared, streams, tol = prepare_serving(args, eng)
     out = {"workload": "serving_trace_%d_requests" % len(prepared), "requests": len(prepared)}
-    out.update(serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load))
+    served = serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load)
+    lat, arrivals = served.pop("_latencies"), served.pop("_arrivals")
+    out.update(served)
+    # the plain path on the same arrivals, and the served latencies of the same requests
+    pl = plain_trace(eng, prepared, tol, arrivals, args.plain_trace_requests, args.plain_trace_seconds)
+    k = pl["requests"]
+    out["plain"] = pl
+    out["served_same_requests"] = {"requests": k, "p50_latency_s": float(np.percentile(lat[:k], 50)),
+                                   "p99_latency_s": float(np.percentile(lat[:k], 99))}
     out.update({"grids": [list(g) for g in workloads.SERVING_GRIDS], "nt_values": list(workloads.SERVING_NT),
                 "seismograms": "ZFP tol 1e-4 streams, decoded on the server's host threads",
                 "zfp_bytes_total": int(sum(len(x) for x in streams.values())),
                 "ring_precisions": ["fp32", "bf16"]})
     if args.serve_load_high > 0:
-        out["high_load"] = serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load_high)
+        hl = serve_trace(args, eng, prepared, tol, capacity_gcells, args.serve_load_high)
+        hl.pop("_latencies")
+        hl.pop("_arrivals")
+        out["high_load"] = hl
     plain, n = plain_on_requests(eng, prepared, tol)
     out["plain_value_same_requests"] = plain
     out["plain_sample"] = n
@@ -720,9 +779,10 @@ def run_gpu(args):
         plan.forward(d_vel, d_wav)
         plan.adjoint(d_seis, d_img, d_slf)
 
-    # Sampled kernel timing (every 16th step's k_step bracketed by CUDA events) is switched
-    # on before the warm-up, so the time-loop graphs are captured with those events outside
-    # the timed region; the timed migrations replay them.
+    # Sampled kernel timing (of every 16 steps, 8 consecutive k_step launches bracketed by one
+    # pair of CUDA events on the plan's stream, so that they keep their programmatic overlap)
+    # is switched on before the warm-up, so the time-loop graphs are captured with those
+    # events outside the timed region; the timed migrations replay them.
     plan.profile(16)
     torch.cuda.synchronize()
     for _ in range(args.warmup):
@@ -781,6 +841,31 @@ def run_gpu(args):
             e2e_ms.append(dt)
     e2e_total = reduce_over_ranks(float(sum(e2e_ms)), "max", ws, "cuda")
     e2e_value = ws * args.steps * cells / (e2e_total * 1e-3) / 1e9
+    # the same with the seismogram as the ZFP tol 1e-4 stream the workload specifies: decoded
+    # on a host thread while the forward pass runs (rtm_migrate_shot_zfp)
+    zfp_tol = 1e-4
+    zstream = eng.zfp_encode(seis, zfp_tol)
+    zfp_ms = []
+    for i in range(1 + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.migrate_shot_zfp(p, ext, wav, zstream, zfp_tol)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i > 0:
+            zfp_ms.append(dt)
+    zfp_total = reduce_over_ranks(float(sum(zfp_ms)), "max", ws, "cuda")
+    t0 = time.perf_counter()
+    eng.zfp_decode(zstream, p.rec_count, p.nt, zfp_tol)
+    decode_ms = (time.perf_counter() - t0) * 1e3
+    e2e_zfp = {"value": ws * args.steps * cells / (zfp_total * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+               "ms_per_step": zfp_total / args.steps, "entry_point": "rtm_migrate_shot_zfp",
+               "zfp_tolerance": zfp_tol, "stream_bytes": len(zstream),
+               "host_decode_ms": decode_ms,
+               "h2d_bytes_per_step": int(ext.nbytes + wav.nbytes + seis.nbytes),
+               "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
+               "note": "the stream in host memory; decode (one host thread, serial: the 0.5.5 stream "
+                       "has no block offsets) overlapped with the forward pass; timed per migration"}
     # sanity: the device-resident and host paths produce the same image
     dev_img = d_img.cpu().numpy()
     agree = float(np.linalg.norm(dev_img - img_h) / max(np.linalg.norm(img_h), 1e-30))
@@ -811,8 +896,10 @@ def run_gpu(args):
                 "avg_launch_ms": bwd_avg_ms, "sampled_launches": prof["bwd_n"],
                 "fwd_kernel_avg_launch_ms": fwd_avg_ms,
                 "fwd_kernel_achieved_gbs": nbytes["k_step_fwd"] / (fwd_avg_ms * 1e-3) / 1e9,
-                "note": "fields stream from HBM every step (warm-cache ncu: 37 MB read per "
-                        "forward step, L2 hit rate 47%); traffic: cold-cache ncu reads"}
+                "timing": "CUDA events on the plan's stream around blocks of 8 consecutive launches "
+                          "(of every 16 steps) inside the time-loop graph; avg = block time / launches",
+                "note": "the step kernel updates the CPML psi itself (no separate psi kernel); "
+                        "traffic: cold-cache ncu reads of one launch"}
     served = None
     if ws == 1 and args.serve_requests > 0:
         cap = batched["value"] if batched else value
@@ -839,6 +926,7 @@ def run_gpu(args):
                     "h2d_bytes_per_step": int(ext.nbytes + wav.nbytes + seis.nbytes),
                     "d2h_bytes_per_step": int(2 * p.nx * p.nz * 4),
                     "entry_point": "rtm_migrate_shot", "image_agreement_rel_l2": agree},
+            "e2e_zfp": e2e_zfp,
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
             "clocks": sampler.summary(), "precision": precision, "batched": batched, "served": served,
             "parity": parity}

@@ -141,6 +141,13 @@ int rtm_stack_transfers(const rtm_stack *stack, long long *d2h_copies, long long
 /* Forward + adjoint of one shot in one call (rtm_iso2d.c:85-93 without the decode). */
 int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wavelet,
                      const float *seismogram, float *image, float *self_image);
+/* The same with the seismogram as the ZFP fixed-accuracy stream the reference reads
+ * (rtm_iso2d.c:85-93 with its zfp2d_lossyDecompression, compression_tools.c:78-135): a host
+ * thread decodes it (rtm_zfp_decode_float2d) while the forward pass runs on the GPU; the
+ * adjoint pass starts once both are done.  RTM_ERR_DECODE for a stream that ends early. */
+int rtm_migrate_shot_zfp(const rtm_params *p, const float *velocity, const float *wavelet,
+                         const void *zfp_stream, size_t zfp_bytes, float tol, float *image,
+                         float *self_image);
 
 /* Forward modelling with trace recording: seismogram[irec*nt + t] = u at the receiver
  * cells after step t's source injection.  (Not in the reference, whose
@@ -291,10 +298,12 @@ int rtm_server_kernel_ms(const rtm_server *server, double *tile_kernel_ms);
  * CPML thicker than 512 cells, is rejected with RTM_ERR_INVALID and a message naming the
  * bytes needed -- e.g. a 400 x 200 model with nt = 2000 and ring storage fits (~52 MB).
  * The first call on each device looks up the array's device address (cudaGetSymbolAddress,
- * with that device current); make that first call before any stream capture.
+ * with that device current); make that first call on a device before any stream capture
+ * begins there.
  * All calls on a device share the array and each call rebuilds what it needs, so calls run
  * one at a time: calls that overlap on the GPU (other streams, other host threads) race.
- * stream: cudaStream_t to run on (NULL = default stream); the call returns when done. */
+ * stream: cudaStream_t to run on (NULL = default stream).  Every call waits for its work on
+ * `stream` to finish before it returns, whether it succeeds or fails. */
 int rtm_migrate_shot_static(const rtm_params *p, const void *d_velocity, const void *d_wavelet,
                             const void *d_seismogram, void *d_image, void *d_self_image,
                             void *stream);

@@ -8,7 +8,7 @@ from .capi import (COMPUTE_FP32, COMPUTE_FP64, PREC_BF16, PREC_FP16, PREC_FP32, 
                    STORE_SNAPSHOT, Plan, RtmError, RtmParams, RtmSurvey, Server, Stack, adjoint_modeling, autotune,
                    aiso_attenuation_cpml, attenuation_profile_cpml, device_info, extend_matrix,
                    footprint_bytes, forward_modeling, iso_acoustic_wave_equation,
-                   laplacian_filter2D, lib, migrate_shot, model_seismogram,
+                   laplacian_filter2D, lib, migrate_shot, migrate_shot_zfp, model_seismogram,
                    normalized_cross_correlation, params_check, release_cached, routine_batch, routine_last_transfers,
                    routine_run,
                    dropin_lib, zfp_decode, zfp_encode)

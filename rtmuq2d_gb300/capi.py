@@ -146,6 +146,7 @@ def _declare(L):
         "rtm_adjoint_modeling": (C.c_int, [P, C.c_int, ip, fp, fp, fp, fp, fp]),
         "rtm_migrate_shot": (C.c_int, [P, fp, fp, fp, fp, fp]),
         "rtm_model_seismogram": (C.c_int, [P, fp, fp, fp]),
+        "rtm_migrate_shot_zfp": (C.c_int, [P, fp, fp, vp, C.c_size_t, C.c_float, fp, fp]),
         "rtm_iso_acoustic_wave_equation": (C.c_int, [P, fp, fp, fp]),
         "rtm_aiso_attenuation_cpml": (C.c_int, [P, fp, fp, fp] + [fp] * 8 + [fp] * 8),
         "rtm_attenuation_profile_cpml": (None, [P] + [fp] * 8),
@@ -204,7 +205,7 @@ def exported_symbols():
     """Names declared in include/rtm_gpu.h that the binding declares."""
     return ["rtm_params_defaults", "rtm_params_check", "rtm_footprint_bytes", "rtm_status_string",
             "rtm_last_error", "rtm_device_info", "rtm_forward_modeling", "rtm_adjoint_modeling",
-            "rtm_migrate_shot", "rtm_model_seismogram", "rtm_iso_acoustic_wave_equation",
+            "rtm_migrate_shot", "rtm_migrate_shot_zfp", "rtm_model_seismogram", "rtm_iso_acoustic_wave_equation",
             "rtm_aiso_attenuation_cpml", "rtm_attenuation_profile_cpml", "rtm_extend_matrix",
             "rtm_laplacian_filter2D", "rtm_normalized_cross_correlation", "rtm_autotune", "rtm_plan_create",
             "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
@@ -300,6 +301,18 @@ def migrate_shot(p: RtmParams, velocity, wavelet, seismogram):
     slf = np.zeros((p.nx, p.nz), np.float32)
     _check(lib().rtm_migrate_shot(C.byref(p), _fp(_f32(velocity)), _fp(_f32(wavelet)),
                                   _fp(_f32(seismogram)), _fp(img), _fp(slf)))
+    return img, slf
+
+
+def migrate_shot_zfp(p: RtmParams, velocity, wavelet, stream: bytes, tol: float):
+    """migrate_shot with the seismogram as a ZFP fixed-accuracy stream, decoded on a host thread
+    while the forward pass runs; returns (image, self image)."""
+    img = np.zeros((p.nx, p.nz), np.float32)
+    slf = np.zeros((p.nx, p.nz), np.float32)
+    buf = np.frombuffer(bytes(stream), np.uint8)
+    _check(lib().rtm_migrate_shot_zfp(C.byref(p), _fp(_f32(velocity)), _fp(_f32(wavelet)),
+                                      buf.ctypes.data_as(C.c_void_p), buf.size, C.c_float(tol), _fp(img),
+                                      _fp(slf)))
     return img, slf
 
 

@@ -1241,6 +1241,31 @@ int rtm_migrate_shot(const rtm_params *p, const float *velocity, const float *wa
     return st;
 }
 
+int rtm_migrate_shot_zfp(const rtm_params *p, const float *velocity, const float *wavelet,
+                         const void *zfp_stream, size_t zfp_bytes, float tol, float *image,
+                         float *self_image)
+{
+    if (!p || !velocity || !image || !self_image) return fail(RTM_ERR_INVALID, "null argument");
+    if (p->n_wavelet > 0 && !wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
+    if (p->rec_count > 0 && !zfp_stream) return fail(RTM_ERR_INVALID, "null seismogram stream");
+    rtm_plan *P = nullptr;
+    RTM_TRY(acquire_plan(*p, &P));
+    // the host decodes the seismogram on a thread of its own while the forward pass runs
+    const size_t n = (size_t)std::max(p->rec_count, 0) * (size_t)p->nt;
+    std::vector<float> seis(std::max<size_t>(n, 1));
+    int dec_st = RTM_OK;
+    std::thread decoder([&] {
+        if (n) dec_st = rtm_zfp_decode_float2d(zfp_stream, zfp_bytes, tol, p->rec_count, p->nt, seis.data());
+    });
+    int st = forward_host(P, velocity, wavelet, nullptr);
+    decoder.join();
+    if (st == RTM_OK && dec_st != RTM_OK) st = fail(dec_st, "seismogram stream: %s", rtm_status_string(dec_st));
+    if (st == RTM_OK) st = adjoint_host(P, seis.data(), image, self_image);
+    if (st != RTM_OK) cudaStreamSynchronize(P->stream);
+    release_plan(P);
+    return st;
+}
+
 int rtm_model_seismogram(const rtm_params *p, const float *velocity, const float *wavelet,
                          float *seismogram)
 {
@@ -1754,24 +1779,40 @@ extern "C" int rtm_migrate_shot_static(const rtm_params *p, const void *d_veloci
     RTM_TRY(make_maps(&P));
     // what the previous call left in the array: status word and receiver maps are rebuilt;
     // fields, strips and accumulators are zeroed by the forward / adjoint drivers
-    RTM_CUDA(cudaMemsetAsync(P.base + L.status, 0, 256, P.stream));
+    if (cudaMemsetAsync(P.base + L.status, 0, 256, P.stream) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamSynchronize(P.stream);
+        return fail(RTM_ERR_CUDA, "clearing the status word of the static scratch");
+    }
     float ref[8 * RTM_STATIC_MAX_THICK], prof[8 * (RTM_STATIC_MAX_THICK + 16)];
     float *a_l = ref, *b_l = a_l + g.thl, *a_r = b_l + g.thl, *b_r = a_r + g.thr;
     float *a_t = b_r + g.thr, *b_t = a_t + g.thu, *a_b = b_t + g.thu, *b_b = a_b + g.thd;
     rtm_attenuation_profile_cpml(p, a_l, a_r, a_t, a_b, b_l, b_r, b_t, b_b);
     pack_profiles(g, a_l, b_l, a_r, b_r, a_t, b_t, a_b, b_b, prof);
-    RTM_CUDA(cudaMemcpyAsync(P.base + L.prof, prof, sizeof(float) * (size_t)prof_layout(g).total,
-                             cudaMemcpyHostToDevice, P.stream));
-    int *rec = P.at<int>(L.rec);
-    k_rec_maps<<<(g.dimx + 127) / 128, 128, 0, P.stream>>>(g, p->rec_first, p->rec_spacing, p->rec_count,
-                                                            rec, rec + g.dimx, rec + 2 * g.dimx);
-    RTM_CUDA(cudaGetLastError());
-    RTM_TRY(dispatch_forward(&P, static_cast<const float *>(d_velocity), g.dimz,
-                             static_cast<const float *>(d_wavelet), nullptr));
-    RTM_TRY(dispatch_adjoint(&P, static_cast<const float *>(d_seismogram)));
-    RTM_TRY(image_to(&P, 0, d_image, 0, 0));
-    RTM_TRY(image_to(&P, 1, d_self_image, 0, 0));
-    return check_status(&P);
+    if (cudaMemcpyAsync(P.base + L.prof, prof, sizeof(float) * (size_t)prof_layout(g).total,
+                        cudaMemcpyHostToDevice, P.stream) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamSynchronize(P.stream);
+        return fail(RTM_ERR_CUDA, "uploading the CPML profiles to the static scratch");
+    }
+    // From the first enqueued operation on, a failure waits for what is already queued on the
+    // stream before it returns, so that nothing of this call still writes the shared array
+    // when the next call starts.
+    auto run = [&]() -> int {
+        int *rec = P.at<int>(L.rec);
+        k_rec_maps<<<(g.dimx + 127) / 128, 128, 0, P.stream>>>(g, p->rec_first, p->rec_spacing, p->rec_count,
+                                                                rec, rec + g.dimx, rec + 2 * g.dimx);
+        RTM_CUDA(cudaGetLastError());
+        RTM_TRY(dispatch_forward(&P, static_cast<const float *>(d_velocity), g.dimz,
+                                 static_cast<const float *>(d_wavelet), nullptr));
+        RTM_TRY(dispatch_adjoint(&P, static_cast<const float *>(d_seismogram)));
+        RTM_TRY(image_to(&P, 0, d_image, 0, 0));
+        RTM_TRY(image_to(&P, 1, d_self_image, 0, 0));
+        return check_status(&P);
+    };
+    const int st = run();
+    if (st != RTM_OK) cudaStreamSynchronize(P.stream);
+    return st;
 }
 
 #include "rtm_serve.cuh"

@@ -201,6 +201,12 @@ def test_small_workload_through_zfp_matches_oracle(engine, oracle, small_workloa
     assert rel_l2(img, ref_img) <= 1e-4 and rel_l2(slf, ref_slf) <= 1e-4
     img, slf = engine.migrate_shot(p, ext, wav, dec)
     assert rel_l2(img, ref_img) <= 1e-4 and rel_l2(slf, ref_slf) <= 1e-4
+    # the host entry point taking the stream itself (decoded on a host thread meanwhile)
+    zimg, zslf = engine.migrate_shot_zfp(p, ext, wav, stream, tol)
+    assert np.array_equal(zimg, img) and np.array_equal(zslf, slf)
+    with pytest.raises(engine.RtmError) as e:
+        engine.migrate_shot_zfp(p, ext, wav, stream[: len(stream) // 3], tol)
+    assert e.value.status == 7                   # RTM_ERR_DECODE
 
 
 @pytest.mark.parametrize("storage", (0, 1))

@@ -6,6 +6,8 @@ implicit device synchronisation).
 Called through the C ABI twice in a row -- the second call reuses what the first left in the
 shared array -- and compared with the existing plan entry points (rtm_plan_create / _forward /
 _adjoint) on the same inputs, within the image tolerance of the parity tests (rel-L2 1e-4).
+Before those two calls, a call of another configuration (a smaller grid with BF16 ring
+storage) leaves other contents at other offsets of the array.
 This file sorts last so that a run stopping at the first failure has run every other test.
 """
 import ctypes as C
@@ -54,6 +56,16 @@ def test_static_scratch_migration_matches_plan_entry_points():
     plan.sync()
     plan.close()
     assert float(ref_img.abs().max()) > 0
+
+    # another layout first: smaller grid, shorter time axis, 16-bit ring storage
+    q = workloads.params_small(nx=240, nz=120, shot_x=120, rec_count=240, nt=400, precision=eng.PREC_BF16)
+    qv = torch.from_numpy(eng.extend_matrix(q, mig[:240, :120])).cuda()
+    qs = torch.from_numpy(np.ascontiguousarray(seis[:240, :400])).cuda()
+    qi = torch.empty((q.nx, q.nz), dtype=torch.float32, device="cuda")
+    qsl = torch.empty_like(qi)
+    st = fn(C.byref(q), qv.data_ptr(), dw.data_ptr(), qs.data_ptr(), qi.data_ptr(), qsl.data_ptr(), None)
+    assert st == 0, lib.rtm_last_error().decode()
+    assert bool(torch.isfinite(qi).all())
 
     for call in range(2):
         img = torch.full((p.nx, p.nz), float("nan"), dtype=torch.float32, device="cuda")
