@@ -181,20 +181,6 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
     const bool inBa = own && !inTa && zq >= g.zb0;
     const T h1 = a.h1, h2 = a.h2, h3 = a.h3;
 
-    // ---- z-strip loads (previous psi, xi) of both columns, issued first
-    T psZ[RXC][4], xZ[RXC][4];
-#pragma unroll
-    for (int r = 0; r < RXC; ++r) {
-        const int x = x0 + warp * RXC + r;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) { psZ[r][j] = (T)0; xZ[r][j] = (T)0; }
-        if (tZ && (inTa || inBa) && x < g.dimx) {
-            const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
-            ld4((inTa ? a.psi_t : a.psi_b) + o, psZ[r]);
-            if (qT || qB) ld4((inTa ? a.xi_t : a.xi_b) + o, xZ[r]);
-        }
-    }
-
     // ---- x-strips
     T dX[RXC][4];
     bool cX[RXC];
@@ -304,6 +290,23 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
                 }
             }
             st4(xi + zq, xX[r]);
+        }
+    }
+
+    // ---- z-strip loads (previous psi, xi) of both columns.  On the top and bottom tiles they
+    // are the pass's first loads; on the corner tiles they follow the x-strips, whose
+    // registers they would otherwise share (loaded before them, they pushed the backward
+    // kernel into spilling: 27.0 -> 29.4 us per backward step on 3400 x 700)
+    T psZ[RXC][4], xZ[RXC][4];
+#pragma unroll
+    for (int r = 0; r < RXC; ++r) {
+        const int x = x0 + warp * RXC + r;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { psZ[r][j] = (T)0; xZ[r][j] = (T)0; }
+        if (tZ && (inTa || inBa) && x < g.dimx) {
+            const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
+            ld4((inTa ? a.psi_t : a.psi_b) + o, psZ[r]);
+            if (qT || qB) ld4((inTa ? a.xi_t : a.xi_b) + o, xZ[r]);
         }
     }
 
@@ -654,13 +657,14 @@ __global__ void __launch_bounds__(WARPS * 32, (sizeof(T) == 4 && WARPS <= 8) ? 2
     // boundary tiles b, b + G, ... (the slow ones: CPML, ring, source, receivers), then its
     // share of the interior tiles.  The r = nb mod G CTAs that carry one boundary tile more
     // take kBalance interior tiles fewer, a boundary tile counting as 1 + kBalance interior
-    // ones.  The interior goes out in rounds -- round j gives one tile to every CTA with more
+    // ones (measured per class with clock64 on 3400 x 700: a boundary tile costs 4.1-5.8
+    // interior ones forward, 2.7-4.4 backward; 5 and 3 were the fastest weights).  The interior goes out in rounds -- round j gives one tile to every CTA with more
     // than j interior tiles, in CTA order -- so that all CTAs sweep the grid together (their
     // halos and, backward, the image and source rows stay in L2).  Measured on 3400 x 700
     // against plain round-robin: forward 24.5 -> 22.6 us, backward 38.2 -> 30.9 us per step.
     // Every tile is taken exactly once.  A stage with no tile left still completes its
     // barrier phase.
-    constexpr int kBalance = BWD ? 2 : 3;
+    constexpr int kBalance = BWD ? 2 : 4;
     const int G = gridDim.x, b = blockIdx.x;
     const int nb = boundary_tiles(g), ni = g.tiles - nb;
     const int r = nb % G;
