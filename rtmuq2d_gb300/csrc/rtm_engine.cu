@@ -679,10 +679,11 @@ static int run_forward(rtm_plan *P, const float *d_vel, int vel_pitch, const flo
             if (d_seis_out && g.nrec > 0) f |= F_RECORD;
             a.store = nullptr;
             a.store_scale = nullptr;
-            if (ring) {                  // slot t + 1 holds the ring of u_{t+1}
-                f |= F_RING_SAVE;
-                a.store = slot_ptr(P, t + 1);
-                a.store_scale = scale_ptr(P, t + 1);
+            if (ring) {                  // slot k holds the ring of u_k: full-precision rings
+                f |= F_RING_SAVE;        // are saved from u_t (step t), 16-bit ones from u_{t+1}
+                const int slot = P->p.precision == RTM_PREC_FP32 ? t : t + 1;
+                a.store = slot_ptr(P, slot);
+                a.store_scale = scale_ptr(P, slot);
             } else if (t % g.slices == 0) {
                 f |= F_SNAP_SAVE;
                 a.store = slot_ptr(P, t / g.slices);

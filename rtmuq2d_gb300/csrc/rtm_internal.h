@@ -22,7 +22,8 @@ constexpr int RXC = 2;                // x columns per thread
 enum : int {
     F_SRC = 1 << 0,          // add wavelet[t]*coef at the shot cell (forward)
     F_RECORD = 1 << 1,       // record u at receiver cells (forward)
-    F_RING_SAVE = 1 << 2,    // save the boundary ring of u_next (forward, ring storage)
+    F_RING_SAVE = 1 << 2,    // save the boundary ring (forward, ring storage): of u_cur at full
+                             // precision, of u_next in 16 bits
     F_SNAP_SAVE = 1 << 3,    // save the interior of u_next (forward, snapshot storage)
     F_OVERWRITE = 1 << 4,    // overwrite receiver cells with the seismogram (backward)
     F_RECON = 1 << 5,        // reconstruct the source field one step back (backward)
