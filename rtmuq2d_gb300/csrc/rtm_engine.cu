@@ -158,7 +158,10 @@ static Geom make_geom(const rtm_params &p, bool batched = false)
     g.zs = p.shot_z + g.thu;
     g.zrec = g.thu + p.rec_depth;
     g.rx0 = g.thl - 4; g.rx1 = g.dimx - g.thr + 4;
-    g.rz0 = g.thu - 4; g.rz1 = g.dimz - g.thd + 4;
+    // z bounds of the reconstruction region on quad boundaries (inside the stencil-only rows
+    // [th_up - 4, dimZ - th_down + 4), still covering the model rows): every ring band is
+    // whole 4-cell quads
+    g.rz0 = round_up(g.thu - 4, 4); g.rz1 = (g.dimz - g.thd + 4) & ~3;
     g.ring_w = g.rx1 - g.rx0 + 8;
     g.ring_h = g.rz1 - g.rz0;
     g.ring_cells = 8 * g.ring_w + 8 * g.ring_h;

@@ -386,57 +386,26 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
     }
 }
 
-// Full-precision ring save of one column of the current field u_t (forward, ring storage),
-// from the thread's quad of the column as the stencil reads it: slot t holds the ring of u_t.
-// The top and bottom bands keep 4 consecutive z cells per column, which two neighbouring lanes
-// hold: the lower lane gathers them with shuffles and writes one 16-byte vector.  The side
-// bands run along z: each lane writes its quad with the widest aligned stores.  x depends
-// only on the warp, so control flow is uniform over a warp around the shuffles.  Saving u_t
-// in the stencil pass, where few registers are live, instead of u_{t+1} after the CPML pass
-// took the forward step from 19.3 to ... us (3400 x 700).
+// Full-precision ring save of the thread's quad of one column of the current field u_t
+// (forward, ring storage), as the stencil reads it: slot t holds the ring of u_t.  The region's
+// z bounds are quad-aligned, so a quad is either wholly in a ring band or not: one 16-byte
+// store.  Saving u_t in the stencil pass, where few registers are live, rather than u_{t+1}
+// after the CPML pass, and without per-cell index arithmetic, took the forward step on
+// 3400 x 700 from 20.0 to ... us.
 template <typename T>
-__device__ __forceinline__ void ring_save_col(const StepArgs<T> &a, const T (&q)[4], int x, int z0, int zend,
-                                              int lane)
+__device__ __forceinline__ void ring_save_quad(const StepArgs<T> &a, const T (&q)[4], int x, int zq)
 {
     const Geom &g = a.g;
-    if (x < g.rx0 - 4 || x >= g.rx1 + 4) return;
+    if (x < g.rx0 - 4 || x >= g.rx1 + 4 || zq < g.rz0 - 4 || zq >= g.rz1 + 4) return;
     T *ring = reinterpret_cast<T *>(a.store);
-    const int zq = z0 + 4 * lane;
-#pragma unroll
-    for (int band = 0; band < 2; ++band) {          // top: [rz0-4, rz0); bottom: [rz1, rz1+4)
-        const int zr = band ? g.rz1 : g.rz0 - 4;
-        if (zr < z0 || zr + 4 > zend) continue;      // each band lies inside one z-tile
-        T nx[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) nx[j] = __shfl_down_sync(0xffffffffu, q[j], 1);
-        const int o = (zr - z0) & 3;
-        if (lane == (zr - z0) >> 2) {
-            T out[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int i = o + k;
-                out[k] = i == 0 ? q[0] : i == 1 ? q[1] : i == 2 ? q[2] : i == 3 ? q[3]
-                       : i == 4 ? nx[0] : i == 5 ? nx[1] : nx[2];
-            }
-            st4(ring + (size_t)band * 4 * g.ring_w + (size_t)(x - (g.rx0 - 4)) * 4, out);
-        }
-    }
-    if (x >= g.rx0 && x < g.rx1) return;
-    // side bands: [rz0, rz1) of the 4 columns either side of the region
-    const size_t base = (size_t)8 * g.ring_w +
-                        (x < g.rx0 ? (size_t)(x - (g.rx0 - 4)) * g.ring_h
-                                   : (size_t)4 * g.ring_h + (size_t)(x - g.rx1) * g.ring_h);
-    const int lo = max(max(zq, g.rz0), z0), hi = min(min(zq + 4, g.rz1), zend);
-    if (lo >= hi) return;
-    T *dst = ring + base + (lo - g.rz0);
-    const int n = hi - lo, j0 = lo - zq;
-    if (n == 4 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
-        st4(dst, q);
-    } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (j >= j0 && j < j0 + n) dst[j - j0] = q[j];
-    }
+    size_t o;
+    if (zq < g.rz0) o = (size_t)(x - (g.rx0 - 4)) * 4;                                 // top band
+    else if (zq >= g.rz1) o = (size_t)4 * g.ring_w + (size_t)(x - (g.rx0 - 4)) * 4;    // bottom
+    else if (x < g.rx0) o = (size_t)8 * g.ring_w + (size_t)(x - (g.rx0 - 4)) * g.ring_h + (zq - g.rz0);
+    else if (x >= g.rx1)
+        o = (size_t)8 * g.ring_w + (size_t)4 * g.ring_h + (size_t)(x - g.rx1) * g.ring_h + (zq - g.rz0);
+    else return;
+    st4(ring + o, q);
 }
 
 template <typename T, int BWD, int WARPS>
@@ -502,7 +471,7 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, T *stage, int t,
             ld4(sprv + (row0 + r) * TZ + 4 * lane, prv);
             ld4(scf + (row0 + r) * TZ + 4 * lane, cf);
             const int x = xb + r;
-            if (!BWD && ring_t && a.store_prec == 0) ring_save_col<T>(a, W[4], x, z0, min(z1, g.dimz), lane);
+            if (!BWD && ring_t && a.store_prec == 0 && zok) ring_save_quad<T>(a, W[4], x, zq);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const T s = cf[j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - prv[j];
