@@ -141,6 +141,99 @@ __device__ __forceinline__ void psi_x_new(const T (&W)[9][4], T (&ps)[4], T ab, 
         if (zq + j >= 4 && zq + j < dimz - 4) ps[j] = bb * ps[j] + ab * d1x_w<T>(W, j) * h1;
 }
 
+// z-strips of a top or bottom tile that touches no x-strip, one column per thread: the band's
+// nq <= 16 quads of a column go to a half-warp (lanes 0-15: the warp's first column, 16-31:
+// its second), rather than both columns to the lanes that own the quads, which on a tile
+// holding a 13-quad band left 19 of 32 lanes idle through the whole correction.  The same
+// arithmetic as cpml_fused's z-strip part (absorbingBoundaryCondition.c:219-263, 312-357): psi
+// of the quad from the tile's z line, the neighbours' psi by shuffles within the half-warp,
+// then xi and the correction term, which goes back by shuffle to the lane that owns the quad
+// and is added to v there.  qb: the band's first quad in the tile; top: the top band.
+template <typename T, int WARPS>
+__device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, const T *scf, T (&v)[RXC][4],
+                                            int x0, int z0, int qb, int nq, bool top)
+{
+    static_assert(RXC == 2, "one column per half-warp");
+    const Geom &g = a.g;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k = lane & 15, c = warp * RXC + (lane >> 4), x = x0 + c;
+    const bool act = k < nq && x < g.dimx;               // (column, quad) in the band's array
+    const int qi = qb + min(k, nq - 1), zq = z0 + 4 * qi;
+    const T h1 = a.h1, h2 = a.h2, h3 = a.h3;
+    const int zlo = top ? 4 : g.dimz - g.thd + 4, zhi = top ? g.thu - 4 : g.dimz - 4;
+    const bool qC = zq + 4 > zlo && zq < zhi;            // the quad holds correction rows
+    const size_t o = top ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
+    T ps[4] = {(T)0, (T)0, (T)0, (T)0}, xz[4] = {(T)0, (T)0, (T)0, (T)0};
+    float aa[4] = {0.f, 0.f, 0.f, 0.f}, bz[4] = {0.f, 0.f, 0.f, 0.f};
+    if (act) {
+        ld4((top ? a.psi_t : a.psi_b) + o, ps);
+        if (qC) ld4((top ? a.xi_t : a.xi_b) + o, xz);
+        const float4 av = *reinterpret_cast<const float4 *>(top ? a.a_t + zq : a.a_b + (zq - g.zb0));
+        const float4 bv = *reinterpret_cast<const float4 *>(top ? a.b_t + zq : a.b_b + (zq - g.zb0));
+        aa[0] = av.x; aa[1] = av.y; aa[2] = av.z; aa[3] = av.w;
+        bz[0] = bv.x; bz[1] = bv.y; bz[2] = bv.z; bz[3] = bv.w;
+    }
+    T zz[12];
+    {
+        const int zi = 4 * qi + HALO;
+        T c4[4];
+        ld4(su + (c + HALO) * SZ + zi, c4);
+        z_line<T>(su, c + HALO, zi, c4, zz);
+    }
+    if (act) {
+        if (x >= 4 && x < g.dimx - 4) {                   // psi cells: x in [4, dimX-4)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int z = zq + j;
+                if (z >= zlo && z < zhi) ps[j] = (T)bz[j] * ps[j] + (T)aa[j] * dpsi_z<T>(zz, j) * h1;
+            }
+        }
+        st4((top ? a.psn_t : a.psn_b) + o, ps);
+    }
+    T q[12];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const T up = __shfl_up_sync(0xffffffffu, ps[j], 1, 16);
+        const T dn = __shfl_down_sync(0xffffffffu, ps[j], 1, 16);
+        q[j] = k > 0 ? up : (T)0;
+        q[4 + j] = ps[j];
+        q[8 + j] = k < 15 ? dn : (T)0;
+    }
+    T dZ[4] = {(T)0, (T)0, (T)0, (T)0};
+    if (act && qC && (top || (x >= 4 && x < g.dimx - 4))) {   // the top rows cover every column
+        T cf[4];
+        ld4(scf + c * TZ + 4 * qi, cf);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int z = zq + j;
+            if (z >= zlo && z < zhi) {
+                const T dp = dpsi_z<T>(q, j) * h1;
+                const T xn = (T)bz[j] * xz[j] + (T)aa[j] * (d2z_q<T>(zz, j) * h3 + dp);
+                xz[j] = xn;
+                dZ[j] = (cf[j] * h2) * (dp + xn);
+            }
+        }
+        st4((top ? a.xi_t : a.xi_b) + o, xz);
+    }
+    // the correction terms back to the lanes owning the quads (lane = quad of the tile)
+    const int kk = lane - qb;
+    const bool mine = kk >= 0 && kk < nq;
+    const int src = mine ? kk : 0;
+    const int zo = z0 + 4 * lane;
+    const bool qCo = zo + 4 > zlo && zo < zhi;
+#pragma unroll
+    for (int r = 0; r < RXC; ++r) {
+        T d[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j] = __shfl_sync(0xffffffffu, dZ[j], 16 * r + src);
+        const int xo = x0 + warp * RXC + r;
+        if (mine && qCo && xo < g.dimx && (top || (xo >= 4 && xo < g.dimx - 4))) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[r][j] = v[r][j] + d[j];
+        }
+    }
+}
+
 // The CPML update of a tile touching a strip, on the stencil results v of the thread's own
 // cells (RXC columns x one 4-cell quad), in registers.  Per strip cell, in the reference's
 // order left, top, right, bottom: dpsi = D1(psi)/dx, xi = b xi + a (D2(u)/dx^2 + dpsi),
@@ -290,6 +383,19 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
                 }
             }
             st4(xi + zq, xX[r]);
+        }
+    }
+
+    // ---- a top or bottom tile without x-strips whose band fits a half-warp
+    if (!tX && tZ) {
+        const bool hasT = z0 < g.thu, hasB = zend > g.zb0;
+        if (hasT != hasB) {
+            const int qb = hasT ? 0 : (max(g.zb0, z0) - z0) >> 2;
+            const int qe = ((hasT ? min(g.thu, zend) : zend) - z0 + 3) >> 2;
+            if (qe - qb <= 16) {
+                cpml_z_half<T, WARPS>(a, su, scf, v, x0, z0, qb, qe - qb, hasT);
+                return;
+            }
         }
     }
 
