@@ -164,8 +164,11 @@ def algorithmic_bytes(p):
     thl, thr, thu, thd = p.th_left, p.th_right, p.th_up, p.th_down
     corr = (thl - 8) * (dz - 8) + (thr - 8) * (dz - 8) + (thu - 8) * dx + (thd - 8) * (dx - 8)
     psi = (thl - 8) * (dz - 8) + (thr - 8) * (dz - 8) + (thu - 8) * (dx - 8) + (thd - 8) * (dx - 8)
-    ring = 8 * (p.nx + 16) + 8 * (p.nz + 8)
-    region = (p.nx + 8) * (p.nz + 8)
+    # reconstruction region: [th_left-4, dimX-th_right+4) x z bounds rounded inward to quads
+    rz0 = (thu - 4 + 3) // 4 * 4
+    rz1 = (dz - thd + 4) // 4 * 4
+    ring = 8 * (p.nx + 16) + 8 * (rz1 - rz0)
+    region = (p.nx + 8) * (rz1 - rz0)
     interior = p.nx * p.nz
     fwd = 16 * cells + 16 * corr + 4 * ring
     bwd = 16 * cells + 16 * corr + 12 * region + 4 * ring + 4 * p.rec_count + 32 * interior / p.time_slices
