@@ -28,7 +28,9 @@ typedef enum rtm_status {
     RTM_ERR_CUDA = 2,         /* a CUDA runtime/driver call failed                    */
     RTM_ERR_NOMEM = 3,        /* device allocation failed or admission refused        */
     RTM_ERR_STATE = 4,        /* call out of order (e.g. adjoint before forward)      */
-    RTM_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (kernel flag)     */
+    RTM_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (kernel flag);
+                                 the results and the device state of the plan, server or
+                                 static array are then undefined: destroy and recreate it */
     RTM_ERR_IO = 6,           /* file missing, short read or write                    */
     RTM_ERR_DECODE = 7,       /* ZFP stream could not be decoded                      */
     RTM_ERR_BUSY = 8          /* serving queue full / result not ready                */
@@ -297,9 +299,10 @@ int rtm_server_kernel_ms(const rtm_server *server, double *tile_kernel_ms);
  * Limit: a configuration whose footprint (rtm_footprint_bytes) exceeds 64 MiB, or with a
  * CPML thicker than 512 cells, is rejected with RTM_ERR_INVALID and a message naming the
  * bytes needed -- e.g. a 400 x 200 model with nt = 2000 and ring storage fits (~52 MB).
- * The first call on each device looks up the array's device address (cudaGetSymbolAddress,
- * with that device current); make that first call on a device before any stream capture
- * begins there.
+ * The call cannot be made on a stream that is being captured into a CUDA graph: it copies
+ * host data, reads its status word back and synchronises the stream.  The first call on each
+ * device also looks up the array's device address (cudaGetSymbolAddress, with that device
+ * current).
  * All calls on a device share the array and each call rebuilds what it needs, so calls run
  * one at a time: calls that overlap on the GPU (other streams, other host threads) race.
  * stream: cudaStream_t to run on (NULL = default stream).  Every call waits for its work on
