@@ -497,6 +497,21 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
 // quad-aligned, so a quad is either wholly in a ring band or not: one 16-byte store.  Saving
 // u_t from the halo tile before the CPML pass, rather than u_{t+1} from registers after it
 // with per-cell index arithmetic, took the forward step on 3400 x 700 from 20.0 to 17.9 us.
+// Ring offset of the quad [zq, zq+4) of column x (ring_index of its first cell), or -1 when
+// the quad holds no ring cell.  With quad-aligned region bounds a quad is either wholly in the
+// ring or not, and its 4 cells are consecutive there (ring_save_quad writes the same offsets).
+__device__ __forceinline__ long long ring_quad_offset(const Geom &g, int x, int zq)
+{
+    if (x < g.rx0 - 4 || x >= g.rx1 + 4 || zq < g.rz0 - 4 || zq >= g.rz1 + 4) return -1;
+    if (zq < g.rz0) return (long long)(x - (g.rx0 - 4)) * 4;                              // top band
+    if (zq >= g.rz1) return (long long)4 * g.ring_w + (long long)(x - (g.rx0 - 4)) * 4;   // bottom
+    if (x < g.rx0) return (long long)8 * g.ring_w + (long long)(x - (g.rx0 - 4)) * g.ring_h + (zq - g.rz0);
+    if (x >= g.rx1)
+        return (long long)8 * g.ring_w + (long long)4 * g.ring_h + (long long)(x - g.rx1) * g.ring_h +
+               (zq - g.rz0);
+    return -1;
+}
+
 template <typename T>
 __device__ __forceinline__ void ring_save_quad(const StepArgs<T> &a, const T (&q)[4], int x, int zq)
 {
@@ -719,12 +734,16 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, T *stage, int t,
                 for (int j = 0; j < 4; ++j)
                     if (zq + j == g.zs) s[j] = add_source<T>(a.wavelet, tsrc, s[j], cf[j]);
             }
-            if (col_ok && ring_t && ring_quad(g, x, zq)) {
+            if (col_ok && ring_t) {
+                const long long o = ring_quad_offset(g, x, zq);
+                if (o >= 0) {
+                    if (a.store_prec == 0) {
+                        ld4(reinterpret_cast<const T *>(a.store) + o, s);
+                    } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int z = zq + j;
-                    const int idx = z < g.dimz ? ring_index(g, x, z) : -1;
-                    if (idx >= 0) s[j] = store_get<T>(a.store, a.store_prec, (size_t)idx, tile_scale);
+                        for (int j = 0; j < 4; ++j)
+                            s[j] = store_get<T>(a.store, a.store_prec, (size_t)o + j, tile_scale);
+                    }
                 }
             }
             if (col_ok) st4(a.s_next + (size_t)x * P + zq, s);
