@@ -66,6 +66,8 @@ def parse():
                     help="serving trace: requests also served one at a time by the plain path")
     ap.add_argument("--plain-trace-seconds", type=float, default=25.0,
                     help="serving trace: wall-time bound of the plain path's run")
+    ap.add_argument("--serve-max-members", type=int, default=1024,
+                    help="resident migrations the server may hold (at most 1024)")
     ap.add_argument("--serve-capacity", type=float, default=150.0,
                     help="with --only served: the batched capacity (Gcell-updates/s) the arrival "
                          "rate is sized by")
@@ -391,7 +393,7 @@ def run_batched(args, eng, rank=0, ws=1):
         dt = time.perf_counter() - t0
         plain = sum(p.cell_updates for p, *_ in sample) / dt / 1e9
     eng.release_cached()
-    srv = eng.Server(0, max_members=min(len(inputs), 128), steps_per_launch=args.steps_per_launch)
+    srv = eng.Server(0, max_members=min(len(inputs), 1024), steps_per_launch=args.steps_per_launch)
     t0 = time.perf_counter()
     ids = [srv.submit(*inp) for inp in inputs]
     # while every member is in its forward pass (they are admitted together), time whole
@@ -506,7 +508,7 @@ def serve_trace(args, eng, prepared, tol, capacity_gcells, load):
         total_hbm = eng.device_info()["hbm_bytes"]
     except Exception:
         total_hbm = None
-    srv = eng.Server(0, max_members=128, steps_per_launch=args.steps_per_launch)
+    srv = eng.Server(0, max_members=args.serve_max_members, steps_per_launch=args.steps_per_launch)
     done, occ, resident, id_to_req = {}, [], [], {}
     t_start = time.monotonic()
     i = 0

@@ -252,7 +252,7 @@ void rtm_release_cached(void);
  * batching).  One thread drives a server. */
 typedef struct rtm_server rtm_server;
 
-/* hbm_budget_bytes <= 0: 80 % of the free device memory.  max_members <= 128. */
+/* hbm_budget_bytes <= 0: 80 % of the free device memory.  max_members <= 1024. */
 int rtm_server_create(long long hbm_budget_bytes, int max_members, int steps_per_launch,
                       rtm_server **server);
 int rtm_server_destroy(rtm_server *server);

@@ -228,6 +228,10 @@ __host__ __device__ __forceinline__ CorrShape corr_shape(const Geom &g)
     return c;
 }
 constexpr int kStripBlock = 256;          // strip items per block (and per 16-bit ring scale)
+// Members whose per-member tables (work-list bases, tile counts, nt, state) the batched
+// kernels stage in shared memory; members beyond it (up to kMaxMembers) are read from the
+// index in global memory, which cost the 64-member ensemble 4% when every member went that way.
+constexpr int kSmemMembers = 128;
 
 __host__ __device__ __forceinline__ int round_block(int n)
 {
@@ -378,8 +382,8 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
                                                         const BMember<T> *__restrict__ mem,
                                                         int2 *__restrict__ state, unsigned *__restrict__ done)
 {
-    __shared__ int s_base[kMaxMembers + 1];
-    __shared__ int2 s_state[kMaxMembers];
+    __shared__ int s_base[kSmemMembers + 1];
+    __shared__ int2 s_state[kSmemMembers];
     __shared__ float red[kStripBlock / 32];
     // The block's member descriptor (all but its tensor maps) in shared memory, so that an
     // item's addresses come from there and its data loads all issue at once.  Consecutive
@@ -396,32 +400,36 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
     };
     // the next step's k_bpsi may launch; it waits for this grid to complete
     griddep_launch();
-    const int nmem = ix->nmem;
-    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->corr_base[k];
-    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
+    // The per-member tables: item bases and the members' (pass, step), staged for the first
+    // kSmemMembers members, read from global memory beyond (state[] is final for this step:
+    // only this grid's last CTA rewrites it, after every CTA is done).
+    const int nmem = ix->nmem, nsm = min(nmem, kSmemMembers);
+    for (int k = threadIdx.x; k <= nsm; k += blockDim.x) s_base[k] = ix->corr_base[k];
+    for (int k = threadIdx.x; k < nsm; k += blockDim.x) s_state[k] = state[k];
     __syncthreads();
-    const int n = s_base[nmem];
+    auto cbase = [&](int k) { return k <= kSmemMembers ? s_base[k] : __ldg(&ix->corr_base[k]); };
+    const int n = cbase(nmem);
     const int stride = gridDim.x * kStripBlock;
     int m = 0, buf = 0;
     if (blockIdx.x * kStripBlock < n) {
-        while (s_base[m + 1] <= blockIdx.x * kStripBlock) ++m;
+        while (cbase(m + 1) <= blockIdx.x * kStripBlock) ++m;
         stage_desc(m, 0);                              // descriptors do not change in a replay
     }
     griddep_wait();                                    // this step's tiles (and psi)
     for (int base = blockIdx.x * kStripBlock; base < n; base += stride) {
         int next_m = m;                                // member of the CTA's next block
         if (base + stride < n)
-            while (s_base[next_m + 1] <= base + stride) ++next_m;
+            while (cbase(next_m + 1) <= base + stride) ++next_m;
         cp_async_wait_all();
         __syncthreads();          // descriptor `buf` visible; the previous block is done with the other
         if (base + stride < n) stage_desc(next_m, buf ^ 1);
-        const int2 st = s_state[m];
+        const int2 st = m < kSmemMembers ? s_state[m] : state[m];
         const BMember<T> &M = *reinterpret_cast<const BMember<T> *>(s_desc[buf]);
         const Geom &g = M.g;
         const bool live = (st.x == 1 || st.x == 2) && st.y < g.nt;
         const CorrShape cs = corr_shape(g);
         const int nstrip = round_block(cs.nA + cs.nB);
-        const int local = base - s_base[m];
+        const int local = base - cbase(m);
         const bool ring = M.storage == 1;
         if (local < nstrip) {
             // ---- corrections (+ ring storage of the forward field)
@@ -496,7 +504,7 @@ __global__ void __launch_bounds__(kStripBlock, 4) k_bstrip(const BatchIndex *__r
     if (s_last) {
         __threadfence();
         for (int k = threadIdx.x; k < nmem; k += blockDim.x) {
-            int2 st = s_state[k];                      // the state this step ran with
+            int2 st = state[k];                        // the state this step ran with
             if (st.x != 1 && st.x != 2) continue;
             const int nt = ix->nt[k];
             ++st.y;
@@ -519,27 +527,28 @@ __global__ void __launch_bounds__(256) k_bpsi(const BatchIndex *__restrict__ ix,
                                               const BMember<T> *__restrict__ mem,
                                               const int2 *__restrict__ state)
 {
-    __shared__ int s_base[kMaxMembers + 1];
-    __shared__ int2 s_state[kMaxMembers];
     // This grid follows the step's k_mstep, which triggers it only after the previous step's
     // k_bstrip has completed: the fields and state read here are final.  k_bstrip may launch.
     griddep_launch();
-    const int nmem = ix->nmem;
-    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) s_base[k] = ix->psi_base[k];
-    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
+    __shared__ int s_base[kSmemMembers + 1];
+    __shared__ int2 s_state[kSmemMembers];
+    const int nmem = ix->nmem, nsm = min(nmem, kSmemMembers);
+    for (int k = threadIdx.x; k <= nsm; k += blockDim.x) s_base[k] = ix->psi_base[k];
+    for (int k = threadIdx.x; k < nsm; k += blockDim.x) s_state[k] = state[k];
     __syncthreads();
-    const int n = s_base[nmem];
+    auto pbase = [&](int k) { return k <= kSmemMembers ? s_base[k] : __ldg(&ix->psi_base[k]); };
+    const int n = pbase(nmem);
     int m = 0;                                         // member of q (monotone in q)
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-        while (s_base[m + 1] <= q) ++m;
-        const int2 st = s_state[m];                    // (pass, t)
+        while (pbase(m + 1) <= q) ++m;
+        const int2 st = m < kSmemMembers ? s_state[m] : state[m];   // (pass, t)
         if (st.x != 1 && st.x != 2) continue;
         const BMember<T> &M = mem[m];
         const Geom &g = M.g;
         if (st.x == 2 && st.y >= g.nt) continue;          // image-only step: no propagation
         int cnt[4];
         psi_counts(g, cnt);
-        int lq = q - s_base[m], strip = 0;
+        int lq = q - pbase(m), strip = 0;
         while (strip < 3 && lq >= cnt[strip]) lq -= cnt[strip++];
         const T *u = st.x == 1 ? M.u[st.y & 1] : M.r[st.y & 1];
         const bool fresh = st.y == 0;
@@ -577,23 +586,30 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
     __shared__ int tile_of[NS], role_of[NS], args_of[NS];
     __shared__ MArgs<T> sargs[2];
     __shared__ float red[MWARPS];
-    // The work lists and the members' (pass, step) of this launch, staged once.  state[] is
-    // final here: this grid launches after k_bpsi of this step passed its wait on the
-    // previous step, and this grid's last CTA rewrites state[] only after every CTA is done.
-    __shared__ int s_base1[kMaxMembers + 1], s_base2[kMaxMembers + 1];
-    __shared__ short s_tiles[kMaxMembers], s_nb[kMaxMembers];
-    __shared__ int s_nt[kMaxMembers];
-    __shared__ int2 s_state[kMaxMembers];
-    const int nmem = ix->nmem;
-    for (int k = threadIdx.x; k <= nmem; k += blockDim.x) {
-        s_base1[k] = ix->base1[k];
-        s_base2[k] = ix->base2[k];
+    // The work lists and the members' (pass, step) of this launch, staged once for the first
+    // kSmemMembers members (read from global memory beyond).  state[] is final here: this
+    // grid launches after the previous step's k_bstrip completed, whose last CTA rewrote it.
+    const BatchIndex &X = *ix;
+    __shared__ int s_base1[kSmemMembers + 1], s_base2[kSmemMembers + 1];
+    __shared__ short s_tiles[kSmemMembers], s_nb[kSmemMembers];
+    __shared__ int s_nt[kSmemMembers];
+    __shared__ int2 s_state[kSmemMembers];
+    const int nmem = X.nmem, nsm = min(nmem, kSmemMembers);
+    for (int k = threadIdx.x; k <= nsm; k += blockDim.x) {
+        s_base1[k] = X.base1[k];
+        s_base2[k] = X.base2[k];
     }
-    for (int k = threadIdx.x; k < nmem; k += blockDim.x) {
-        s_tiles[k] = (short)ix->tiles[k];
-        s_nb[k] = (short)ix->nb[k];
-        s_nt[k] = ix->nt[k];
+    for (int k = threadIdx.x; k < nsm; k += blockDim.x) {
+        s_tiles[k] = (short)X.tiles[k];
+        s_nb[k] = (short)X.nb[k];
+        s_nt[k] = X.nt[k];
     }
+    auto base1 = [&](int k) { return k <= kSmemMembers ? s_base1[k] : __ldg(&X.base1[k]); };
+    auto base2 = [&](int k) { return k <= kSmemMembers ? s_base2[k] : __ldg(&X.base2[k]); };
+    auto m_tiles = [&](int k) { return k < kSmemMembers ? (int)s_tiles[k] : __ldg(&X.tiles[k]); };
+    auto m_nb = [&](int k) { return k < kSmemMembers ? (int)s_nb[k] : __ldg(&X.nb[k]); };
+    auto m_nt = [&](int k) { return k < kSmemMembers ? s_nt[k] : __ldg(&X.nt[k]); };
+    auto m_state = [&](int k) { return k < kSmemMembers ? s_state[k] : state[k]; };
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
@@ -603,9 +619,9 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
     // only then may this step's k_bpsi launch
     griddep_wait();
     griddep_launch();
-    for (int k = threadIdx.x; k < nmem; k += blockDim.x) s_state[k] = state[k];
+    for (int k = threadIdx.x; k < nsm; k += blockDim.x) s_state[k] = state[k];
     __syncthreads();
-    const int total1 = s_base1[nmem], total = total1 + s_base2[nmem];
+    const int total1 = base1(nmem), total = total1 + base2(nmem);
     // Thread 0 maps the i-th work item of this CTA to (member, role, tile), builds the
     // arguments of (member, role) when they differ from the last item's (in the argument
     // slot the other stage is not using) and starts the stage's TMA loads.
@@ -642,26 +658,27 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
         int m, lt, role;
         bool skip;
         if (tg < total1) {
-            while (s_base1[cur1 + 1] <= tg) ++cur1;
+            while (base1(cur1 + 1) <= tg) ++cur1;
             m = cur1;
-            const int2 st = s_state[m];
-            const int k = tg - s_base1[m], ni = s_tiles[m] - s_nb[m];
+            const int2 st = m_state(m);
+            const int nbm = m_nb(m);
+            const int k = tg - base1(m), ni = m_tiles(m) - nbm;
             skip = st.x != 1 && st.x != 2;               // idle or finished member
             if (k < ni) {
                 role = st.x == 1 ? ROLE_FWD : ROLE_RCV;
-                lt = s_nb[m] + k;
+                lt = nbm + k;
             } else {
                 role = ROLE_SRC;
                 lt = k - ni;
-                skip = skip || st.x != 2 || st.y < 2 || st.y >= s_nt[m];
+                skip = skip || st.x != 2 || st.y < 2 || st.y >= m_nt(m);
             }
         } else {
             const int t2 = tg - total1;
-            while (s_base2[cur2 + 1] <= t2) ++cur2;
+            while (base2(cur2 + 1) <= t2) ++cur2;
             m = cur2;
-            const int2 st = s_state[m];
+            const int2 st = m_state(m);
             role = st.x == 1 ? ROLE_FWD : ROLE_RCV;
-            lt = t2 - s_base2[m];
+            lt = t2 - base2(m);
             skip = st.x != 1 && st.x != 2;
         }
         if (skip) {
@@ -669,7 +686,7 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
             mbar_arrive(&full[s]);
             return;
         }
-        const int2 st = s_state[m];
+        const int2 st = m_state(m);
         const BMember<T> &M = mem[m];
         const int key = m * 4 + role;
         if (key != last_key) {

@@ -191,7 +191,7 @@ struct BMember {                 // aligned like its leading tensor maps
     unsigned *status;
 };
 
-constexpr int kMaxMembers = 128;   // members of one batch
+constexpr int kMaxMembers = 1024;  // members of one batch (the kernels read their tables from global memory)
 constexpr int kBatchTileX = 32;    // x columns per tile of the batched step kernel (MTX)
 
 // Work lists of one batch.  The tile work of a step runs in two phases: first every

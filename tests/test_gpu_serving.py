@@ -217,3 +217,35 @@ def test_server_clear_and_strip_tiles_match_plain_and_oracle(engine, oracle):
         ref_img, ref_slf = oracle.migrate(c[0].as_dict(), c[1], c[2], c[3])
         assert rel_l2(out[rid][0], ref_img) <= 1e-4, rid
         assert rel_l2(out[rid][1], ref_slf) <= 1e-4, rid
+
+
+def test_server_holds_more_than_128_members(engine):
+    """More resident members than the old 128-member limit of the batched kernels' tables:
+    300 short migrations of a small grid (different shots, so different images) admitted
+    together; each image equals the same request migrated alone, bit for bit."""
+    d = load()
+    p0, ext, wav, seis = _shorter(engine, _case(engine, d, "uneven", storage=1), 40)
+    cases = []
+    for k in range(300):
+        p = p0.replace(shot_x=8 + (k * 7) % max(1, p0.nx - 16))
+        if _valid(engine, p):
+            cases.append((p, ext, wav, seis))
+    assert len(cases) >= 200
+    srv = engine.Server(0, max_members=len(cases), steps_per_launch=8)
+    ids = [srv.submit(*c) for c in cases]
+    out, most = {}, 0
+    while True:
+        active, queued = srv.step()
+        most = max(most, active)
+        while True:
+            r = srv.poll()
+            if r is None:
+                break
+            out[r[0]] = r[1:]
+        if active == 0 and queued == 0 and not srv.params:
+            break
+    srv.close()
+    assert most > 128 and len(out) == len(cases)
+    for k in (0, 129, len(cases) - 1):
+        img, slf = _alone(engine, cases[k])[:2]
+        assert np.array_equal(out[ids[k]][0], img) and np.array_equal(out[ids[k]][1], slf), k
