@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--batch-members", type=int, default=64,
                     help="batched UQ ensemble: velocity realizations (0: skip)")
     ap.add_argument("--batch-nt", type=int, default=7500)
+    ap.add_argument("--no-batch-autotune", dest="batch_autotune", action="store_false",
+                    help="batched members at the default 32-column tile width")
     ap.add_argument("--plain-sample", type=int, default=6,
                     help="ensemble members also run one at a time through the plain path")
     ap.add_argument("--serve-requests", type=int, default=96,
@@ -345,8 +347,9 @@ def summary(line):
         for key, name in (("stencil_kernel_roofline", "k_mstep_frac"), ("forward_step_roofline", "fwd_step_frac")):
             if b.get(key):
                 out["batched"][name] = r3(b[key]["frac"])
-        if b.get("autotuned"):
-            out["batched"]["tiles"] = b["autotuned"]
+        if b.get("autotuned_tile_x_by_width_class"):
+            out["batched"]["tile_x_by_width_class"] = {k: v["tile_x"] for k, v in
+                                                       b["autotuned_tile_x_by_width_class"].items()}
     s = line.get("served")
     if s:
         out["served"] = {k: r3(v) for k, v in pick(s, "requests", "value", "p50_latency_s", "p99_latency_s",
@@ -393,9 +396,24 @@ def run_batched(args, eng, rank=0, ws=1):
         dt = time.perf_counter() - t0
         plain = sum(p.cell_updates for p, *_ in sample) / dt / 1e9
     eng.release_cached()
+    # batched autotuner: the tile width (32 or 16 columns) per window-width class (nx to the
+    # nearest 512 columns), timed on 8 copies of the class's middle member with a 40-step
+    # time axis; each member is submitted with its class's width
+    tuned, width = {}, [0] * len(inputs)
+    if args.batch_autotune:
+        classes = {}
+        for i, (p, *_) in enumerate(inputs):
+            classes.setdefault(int(round(p.nx / 512.0)) * 512, []).append(i)
+        for cls, idx in sorted(classes.items()):
+            p_rep = inputs[idx[len(idx) // 2]][0]
+            tx, ms = eng.autotune_batched(p_rep, members=8, steps=40)
+            tuned[str(cls)] = {"tile_x": tx, "tuned_on_nx": p_rep.nx, "members": len(idx),
+                               "ms_per_batched_step_of_8": ms}
+            for i in idx:
+                width[i] = tx
     srv = eng.Server(0, max_members=min(len(inputs), 1024), steps_per_launch=args.steps_per_launch)
     t0 = time.perf_counter()
-    ids = [srv.submit(*inp) for inp in inputs]
+    ids = [srv.submit(inp[0].replace(tile_x=width[i]), *inp[1:]) for i, inp in enumerate(inputs)]
     # while every member is in its forward pass (they are admitted together), time whole
     # batched steps (k_mstep + k_bpsi + k_bstrip) from the server's CUDA events
     # (and the tile kernel alone on one step per replay, k_mstep, timed by the server)
@@ -462,6 +480,7 @@ def run_batched(args, eng, rank=0, ws=1):
             "speedup_vs_plain": value / plain if plain else None,
             "image_agreement_with_plain_rel_l2": agree,
             "steps_per_launch": args.steps_per_launch, "device_bytes": st["bytes_in_use"],
+            "autotuned_tile_x_by_width_class": tuned or None,
             "forward_step_roofline": step_roof,
             "stencil_kernel_roofline": tile_roof,
             "gpu_launches": st["launches"],

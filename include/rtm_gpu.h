@@ -285,6 +285,13 @@ int rtm_server_stats(const rtm_server *server, long long *cell_updates, double *
  * (steps_per_launch >= 2; 0 otherwise).  For the kernel's roofline; the step itself
  * advances every active member as usual. */
 int rtm_server_kernel_ms(const rtm_server *server, double *tile_kernel_ms);
+/* Tile width of the batched kernel (32 or 16 columns) for p's grid shape, chosen by timing
+ * `members` copies of p (nt shortened to `steps`) through a server with each width; later
+ * submissions of that shape with tile_x = 0 use it (tile_x = 16 or 32 in a request forces a
+ * width).  *best_ms_per_step: the batch's GPU time per batched step at that width.  No
+ * counterpart in the reference. */
+int rtm_autotune_batched(const rtm_params *p, int members, int steps, int *best_tile_x,
+                         float *best_ms_per_step);
 
 /* ---- migration without device allocation -------------------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc: a host whose

@@ -5,7 +5,7 @@ include/rtm_gpu.h (librtmgpu.so); ``capi`` is its ctypes binding.  There is no C
 fallback: a missing or unloadable library raises.
 """
 from .capi import (COMPUTE_FP32, COMPUTE_FP64, PREC_BF16, PREC_FP16, PREC_FP32, STORE_RING,
-                   STORE_SNAPSHOT, Plan, RtmError, RtmParams, RtmSurvey, Server, Stack, adjoint_modeling, autotune,
+                   STORE_SNAPSHOT, Plan, RtmError, RtmParams, RtmSurvey, Server, Stack, adjoint_modeling, autotune, autotune_batched,
                    aiso_attenuation_cpml, attenuation_profile_cpml, device_info, extend_matrix,
                    footprint_bytes, forward_modeling, iso_acoustic_wave_equation,
                    laplacian_filter2D, lib, migrate_shot, migrate_shot_zfp, model_seismogram,

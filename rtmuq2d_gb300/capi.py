@@ -165,6 +165,7 @@ def _declare(L):
         "rtm_plan_capture_source": (C.c_int, [vp, C.c_int, ip, vp]),
         "rtm_plan_launch_count": (C.c_longlong, [vp]),
         "rtm_plan_bytes": (C.c_longlong, [vp]),
+        "rtm_autotune_batched": (C.c_int, [P, C.c_int, C.c_int, ip, C.POINTER(C.c_float)]),
         "rtm_release_cached": (None, []),
         "rtm_server_create": (C.c_int, [C.c_longlong, C.c_int, C.c_int, C.POINTER(vp)]),
         "rtm_server_destroy": (C.c_int, [vp]),
@@ -211,7 +212,7 @@ def exported_symbols():
             "rtm_plan_destroy", "rtm_plan_set_stream", "rtm_plan_forward", "rtm_plan_adjoint",
             "rtm_plan_read_field", "rtm_plan_read_image", "rtm_plan_sync", "rtm_plan_capture_source",
             "rtm_plan_launch_count",
-            "rtm_plan_bytes", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
+            "rtm_plan_bytes", "rtm_autotune_batched", "rtm_release_cached", "rtm_plan_profile", "rtm_plan_profile_read",
             "rtm_server_create", "rtm_server_destroy", "rtm_server_submit", "rtm_server_submit_zfp",
             "rtm_server_step",
             "rtm_server_poll", "rtm_server_wait", "rtm_server_stats", "rtm_server_kernel_ms", "rtm_migrate_shot_static",
@@ -453,6 +454,15 @@ def dropin_lib():
     """librtm_dropin.so: the reference's entry-point names over the engine."""
     lib()
     return C.CDLL(_build.DROPIN_LIB)
+
+
+def autotune_batched(p: RtmParams, members: int = 8, steps: int = 40):
+    """Batched tile width (32 or 16) for p's grid shape, used by later server submissions of
+    that shape with tile_x = 0; returns (tile_x, ms per batched step of `members` copies)."""
+    t = C.c_int()
+    ms = C.c_float()
+    _check(lib().rtm_autotune_batched(C.byref(p), int(members), int(steps), C.byref(t), C.byref(ms)))
+    return t.value, ms.value
 
 
 def autotune(p: RtmParams, steps: int = 200):

@@ -708,15 +708,17 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
         role_of[s] = role;
         int xt, zt;
         tile_coords(sargs[last_args].g, lt, xt, zt);
-        const int x0 = xt * MTX, z0 = ztile_origin(sargs[last_args].g, zt);
+        const int tx = sargs[last_args].g.tx;           // the member's tile width (16 or 32)
+        const int x0 = xt * tx, z0 = ztile_origin(sargs[last_args].g, zt);
         const bool rfield = role == ROLE_RCV;
         const CUtensorMap *mc = rfield ? &M.tm_r[l_mu] : &M.tm_u[l_mu];
         const CUtensorMap *mp = rfield ? &M.tm_rp[l_mp] : &M.tm_up[l_mp];
         T *stg = stage0 + (size_t)s * STAGE;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(sizeof(T) * STAGE));
+        const int ut = mstage_ut(tx), pt = tx * TZ;
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(sizeof(T) * mstage_elems(tx)));
         tma_load_2d(stg, mc, z0 - HALO, x0 - HALO, &full[s]);
-        tma_load_2d(stg + UT, mp, z0, x0, &full[s]);
-        tma_load_2d(stg + UT + PT, &M.tm_c, z0, x0, &full[s]);
+        tma_load_2d(stg + ut, mp, z0, x0, &full[s]);
+        tma_load_2d(stg + ut + pt, &M.tm_c, z0, x0, &full[s]);
     };
     if (threadIdx.x == 0) {
         args_of[0] = args_of[1] = 0;
@@ -745,9 +747,15 @@ __global__ void __launch_bounds__(MTHREADS, sizeof(T) == 4 ? 2 : 1)
             const T *stg = stage0 + (size_t)s * STAGE;
             const int role = role_of[s];
             const MArgs<T> *ap = &sargs[args_of[s]];
-            if (role == ROLE_FWD) march_tile<T, ROLE_FWD>(ap, stg, lt, red);
-            else if (role == ROLE_RCV) march_tile<T, ROLE_RCV>(ap, stg, lt, red);
-            else march_tile<T, ROLE_SRC>(ap, stg, lt, red);
+            if (ap->g.tx == MTX) {
+                if (role == ROLE_FWD) march_tile<T, ROLE_FWD, MCW>(ap, stg, lt, red);
+                else if (role == ROLE_RCV) march_tile<T, ROLE_RCV, MCW>(ap, stg, lt, red);
+                else march_tile<T, ROLE_SRC, MCW>(ap, stg, lt, red);
+            } else {
+                if (role == ROLE_FWD) march_tile<T, ROLE_FWD, MCW / 2>(ap, stg, lt, red);
+                else if (role == ROLE_RCV) march_tile<T, ROLE_RCV, MCW / 2>(ap, stg, lt, red);
+                else march_tile<T, ROLE_SRC, MCW / 2>(ap, stg, lt, red);
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) issue(i + NS, s);

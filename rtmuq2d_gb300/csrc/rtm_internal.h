@@ -192,7 +192,7 @@ struct BMember {                 // aligned like its leading tensor maps
 };
 
 constexpr int kMaxMembers = 1024;  // members of one batch (the kernels read their tables from global memory)
-constexpr int kBatchTileX = 32;    // x columns per tile of the batched step kernel (MTX)
+constexpr int kBatchTileX = 32;    // widest tile of the batched step kernel (MTX); members use it or half
 
 // Work lists of one batch.  The tile work of a step runs in two phases: first every
 // member's interior field tiles and source-reconstruction tiles, then every member's field

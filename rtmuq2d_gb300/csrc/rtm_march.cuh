@@ -1,13 +1,14 @@
 // rtm_march.cuh -- tile step of the batched engine (included by rtm_kernels.cu after
 // rtm_step.cuh, whose stencil helpers it shares).
 //
-// A tile is MTX = 32 columns x TZ = 128 z cells of ONE field of one migration.  Its inputs
-// -- the field with a 4-cell halo (MTX+8 rows of SZ), the previous field and coef (MTX rows
-// of TZ) -- arrive in one shared-memory stage by TMA.  Warp w owns columns 4w..4w+3 and
-// marches along x through them with a 9-column register window (1 new row per column);
-// lane l owns the 4 z cells 4l..4l+3 of every column (16-byte vectors).  Each thread thus
-// updates 16 cells per tile, and everything that is decided per tile is decided once for
-// those 16 cells.  A tile reads nothing from global memory: the per-cell work that needs
+// A tile is TX = 8 x CW columns (CW = 4 or 2 columns per warp: 32 or 16, a member's tile
+// width, chosen per grid shape by rtm_autotune_batched) x TZ = 128 z cells of ONE field of one
+// migration.  Its inputs -- the field with a 4-cell halo (TX+8 rows of SZ), the previous field
+// and coef (TX rows of TZ) -- arrive in one shared-memory stage by TMA.  Warp w owns columns
+// CW w .. CW w + CW - 1 and marches along x through them with a 9-column register window
+// (1 new row per column); lane l owns the 4 z cells 4l..4l+3 of every column (16-byte
+// vectors).  Each thread thus updates 4 CW cells per tile, and everything that is decided per
+// tile is decided once for those cells.  A tile reads nothing from global memory: the per-cell work that needs
 // other data -- the CPML corrections of the strips, the boundary ring's storage and
 // restoration -- is done afterwards by the strip kernel k_bstrip (rtm_batch.cuh), over
 // the strip cells only.
@@ -32,8 +33,8 @@
 // reference's operations on a cell.
 
 constexpr int MWARPS = 8;                 // warps per CTA
-constexpr int MCW = 4;                    // columns per warp
-constexpr int MTX = MWARPS * MCW;         // 32 columns per tile
+constexpr int MCW = 4;                    // columns per warp of the widest tile
+constexpr int MTX = MWARPS * MCW;         // 32 columns per tile (the stage is sized for it)
 constexpr int MTHREADS = MWARPS * 32;
 
 // CTA barriers of the tile code (named barrier 1 over the MWARPS warps).
@@ -65,6 +66,9 @@ struct MCfg {
     static constexpr int NS = 2;                           // stages per CTA
     static constexpr size_t SMEM = (size_t)NS * STAGE * sizeof(T);
 };
+// Stage layout of a tile TX columns wide (TX <= MTX): halo tile, previous field, coef.
+__host__ __device__ __forceinline__ int mstage_ut(int tx) { return (tx + 2 * HALO) * SZ; }
+__host__ __device__ __forceinline__ int mstage_elems(int tx) { return mstage_ut(tx) + 2 * tx * TZ; }
 
 // Per (member, role) arguments of a step, built by the issuing thread in shared memory.
 template <typename T>
@@ -97,26 +101,27 @@ __host__ __device__ __forceinline__ float store_scale_of(float mx, int prec)
 // The arguments live in shared memory and the tile stores through generic pointers: the
 // __restrict__ qualifiers tell the compiler that those stores never modify the arguments
 // or the stage, so it keeps argument values in registers across them instead of reloading.
-template <typename T, int ROLE>
+template <typename T, int ROLE, int CW>
 __device__ __forceinline__ void march_tile(const MArgs<T> *__restrict__ ap, const T *__restrict__ stage,
                                            int lt, float *red)
 {
     const MArgs<T> &a = *ap;
-    constexpr int UT = MCfg<T>::UT, PT = MCfg<T>::PT;
+    constexpr int TXW = MWARPS * CW;                 // columns of this tile width
+    constexpr int UT = (TXW + 2 * HALO) * SZ, PT = TXW * TZ;
     const Geom &g = a.g;
     const int flags = a.flags;
-    const T *su = stage;                   // field + halo   [MTX+8][SZ]
-    const T *sprv = stage + UT;            // previous field [MTX][TZ]
-    const T *scf = stage + UT + PT;        // coef           [MTX][TZ]
+    const T *su = stage;                   // field + halo   [TXW+8][SZ]
+    const T *sprv = stage + UT;            // previous field [TXW][TZ]
+    const T *scf = stage + UT + PT;        // coef           [TXW][TZ]
 
     int xt, zt;
     tile_coords(g, lt, xt, zt);
-    const int x0 = xt * MTX, z0 = ztile_origin(g, zt);
-    const int x1 = x0 + MTX, z1 = min(ztile_end(g, zt), z0 + TZ);
+    const int x0 = xt * TXW, z0 = ztile_origin(g, zt);
+    const int x1 = x0 + TXW, z1 = min(ztile_end(g, zt), z0 + TZ);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int zq = z0 + 4 * lane;
-    const int xw = x0 + MCW * warp;        // first column of this warp
-    const int rw = MCW * warp;             // halo-tile row of column xw - 4
+    const int xw = x0 + CW * warp;         // first column of this warp
+    const int rw = CW * warp;              // halo-tile row of column xw - 4
     const int zi = 4 * lane + HALO;
     const bool zok = zq < min(z1, g.dimz);
     const size_t P = (size_t)g.pitch;
@@ -151,7 +156,7 @@ __device__ __forceinline__ void march_tile(const MArgs<T> *__restrict__ ap, cons
     if (fast) {
         // ================= no per-cell decisions =================
 #pragma unroll
-        for (int c = 0; c < MCW; ++c) {
+        for (int c = 0; c < CW; ++c) {
             const int x = xw + c;
             ld4(su + (rw + c + 8) * SZ + zi, W[8]);
             T zz[12];
@@ -187,9 +192,9 @@ __device__ __forceinline__ void march_tile(const MArgs<T> *__restrict__ ap, cons
 
     // ================= tiles with per-cell decisions =================
     float mx = 0.0f;                       // 16-bit snapshots: max |v| over the stored cells
-    T keep[MCW][4];                        // ...and the tile's values until the scale is known
+    T keep[CW][4];                         // ...and the tile's values until the scale is known
 #pragma unroll
-    for (int c = 0; c < MCW; ++c) {
+    for (int c = 0; c < CW; ++c) {
         const int x = xw + c;
         ld4(su + (rw + c + 8) * SZ + zi, W[8]);
         T zz[12];
@@ -267,7 +272,7 @@ __device__ __forceinline__ void march_tile(const MArgs<T> *__restrict__ ap, cons
         const float inv = 1.0f / scale;
         if (threadIdx.x == 0) a.store_scale[lt] = scale;
 #pragma unroll
-        for (int c = 0; c < MCW; ++c)
+        for (int c = 0; c < CW; ++c)
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int x = xw + c, z = zq + j;

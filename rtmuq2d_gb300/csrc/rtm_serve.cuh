@@ -181,9 +181,9 @@ static int admit(rtm_server *S, int m, ServeRequest *R)
         P->own_stream = false;
     }
     const Geom &g = P->g;
-    if (g.tx != kBatchTileX) {            // tensor-map boxes must match the kernel's tiles
+    if (g.tx != kBatchTileX && g.tx != kBatchTileX / 2) {   // tensor-map boxes must match the kernel's tiles
         S->idle.push_back(P);
-        return fail(RTM_ERR_INVALID, "batched member with tile width %d (needs %d)", g.tx, kBatchTileX);
+        return fail(RTM_ERR_INVALID, "batched member with tile width %d (needs %d or %d)", g.tx, kBatchTileX, kBatchTileX / 2);
     }
     cudaStream_t s = S->up;
     float *stage = P->at<float>(P->L.staging);
@@ -378,6 +378,20 @@ static int server_init(rtm_server *S, long long hbm_budget_bytes)
     return RTM_OK;
 }
 
+// ---- batched tile width per grid shape ---------------------------------------------------
+// rtm_autotune_batched's choices (16 or 32 columns), keyed like the single-migration tuner's.
+static std::map<TuneKey, int> g_tuned_batch;   // guarded by g_tune_mutex
+
+// Tile width of a batched member: the request's tile_x when it is one the batched kernel has
+// (16, 32), else the tuned width of its grid shape, else 32.
+static int batched_tile_x(const rtm_params &p)
+{
+    if (p.tile_x == kBatchTileX || p.tile_x == kBatchTileX / 2) return p.tile_x;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned_batch.find(tune_key(p));
+    return it != g_tuned_batch.end() ? it->second : kBatchTileX;
+}
+
 // rtm_server_submit; with `zfp`, the seismogram comes later from a decoder thread.
 static int submit_request(rtm_server *S, const rtm_params *p, const float *velocity, const float *wavelet,
                           const float *seismogram, bool zfp, long long *request_id)
@@ -388,13 +402,13 @@ static int submit_request(rtm_server *S, const rtm_params *p, const float *veloc
     if (p->n_wavelet > 0 && !wavelet) return fail(RTM_ERR_INVALID, "null wavelet");
     if (p->rec_count > 0 && !seismogram && !zfp) return fail(RTM_ERR_INVALID, "null seismogram");
     rtm_params q = *p;
-    q.tile_x = kBatchTileX;
+    q.tile_x = batched_tile_x(*p);
     const long long bytes = (long long)make_layout(q, make_geom(q, true)).total;
     if (bytes > S->budget) return fail(RTM_ERR_NOMEM, "request needs %lld bytes, budget %lld", bytes, S->budget);
     auto *R = new ServeRequest();
     R->id = S->next_id++;
     R->p = *p;
-    R->p.tile_x = kBatchTileX;           // the batched step kernel's tile width
+    R->p.tile_x = q.tile_x;              // the member's tile width in the batched kernel
     const size_t nv = (size_t)(p->th_left + p->nx + p->th_right) * (p->th_up + p->nz + p->th_down);
     R->vel.assign(velocity, velocity + nv);
     if (p->n_wavelet > 0) R->wav.assign(wavelet, wavelet + p->n_wavelet);
@@ -622,6 +636,62 @@ int rtm_server_kernel_ms(const rtm_server *S, double *tile_kernel_ms)
 {
     if (!S || !tile_kernel_ms) return fail(RTM_ERR_INVALID, "null argument");
     *tile_kernel_ms = S->kernel_sampled ? S->kernel_ms_last : 0.0;
+    return RTM_OK;
+}
+
+// Batched tile width for p's grid shape: `members` copies of p (a constant 2000 m/s model,
+// zero seismogram; nt rounded to `steps`) migrated through a server with each tile width the
+// batched kernel has, timed by the server's CUDA events over the batched steps; the faster
+// width is kept for later submissions of that shape (tile_x = 0).
+int rtm_autotune_batched(const rtm_params *p, int members, int steps, int *best_tile_x,
+                         float *best_ms_per_step)
+{
+    NvtxRange range("rtm autotune batched");
+    if (!p) return fail(RTM_ERR_INVALID, "null argument");
+    RTM_TRY(check_params(*p));
+    if (p->compute != RTM_COMPUTE_FP32) return fail(RTM_ERR_INVALID, "the server runs FP32 migrations");
+    if (members < 1 || members > kMaxMembers) return fail(RTM_ERR_INVALID, "members must be in [1, %d]", kMaxMembers);
+    if (steps < 1) return fail(RTM_ERR_INVALID, "steps must be >= 1");
+    rtm_params q = *p;
+    q.nt = (steps + q.time_slices - 1) / q.time_slices * q.time_slices;
+    const size_t nv = (size_t)(q.th_left + q.nx + q.th_right) * (q.th_up + q.nz + q.th_down);
+    std::vector<float> vel(nv, 2000.0f), wav((size_t)std::max(q.n_wavelet, 1), 0.0f);
+    for (size_t k = 0; k < wav.size(); ++k) wav[k] = (float)(k % 7) * 0.1f;
+    std::vector<float> seis((size_t)std::max(q.rec_count, 1) * q.nt, 0.0f);
+    const int cands[2] = {kBatchTileX, kBatchTileX / 2};
+    int best = -1;
+    float best_ms = 0.0f;
+    for (int tx : cands) {
+        q.tile_x = tx;
+        rtm_server *S = nullptr;
+        RTM_TRY(rtm_server_create(0, members, 16, &S));
+        int st = RTM_OK;
+        for (int m = 0; m < members && st == RTM_OK; ++m) {
+            long long id = 0;
+            st = rtm_server_submit(S, &q, vel.data(), wav.data(), seis.data(), &id);
+        }
+        long long polled = 0;
+        while (st == RTM_OK && polled < members) {
+            int active = 0, queued = 0;
+            st = rtm_server_step(S, &active, &queued);
+            long long id = 0;
+            while (st == RTM_OK && rtm_server_poll(S, &id, nullptr, nullptr, nullptr) == RTM_OK) ++polled;
+            if (st == RTM_OK && active == 0 && queued == 0 && polled < members)
+                st = fail(RTM_ERR_STATE, "batched autotune: requests neither resident nor queued");
+        }
+        double ms = 0.0;
+        if (st == RTM_OK) st = rtm_server_stats(S, nullptr, &ms, nullptr, nullptr);
+        rtm_server_destroy(S);
+        if (st != RTM_OK) return st;
+        const float per = (float)(ms / (2.0 * q.nt + 1.0));      // per batched step of the batch
+        if (best < 0 || per < best_ms) { best = tx; best_ms = per; }
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tuned_batch[tune_key(*p)] = best;
+    }
+    if (best_tile_x) *best_tile_x = best;
+    if (best_ms_per_step) *best_ms_per_step = best_ms;
     return RTM_OK;
 }
 

@@ -249,3 +249,26 @@ def test_server_holds_more_than_128_members(engine):
     for k in (0, 129, len(cases) - 1):
         img, slf = _alone(engine, cases[k])[:2]
         assert np.array_equal(out[ids[k]][0], img) and np.array_equal(out[ids[k]][1], slf), k
+
+
+@pytest.mark.parametrize("tile_x", (16, 32))
+def test_server_tile_widths_match_plain(engine, tile_x):
+    """Both tile widths of the batched kernel (the batched autotuner's choices) give the
+    single-migration path's image (rel-L2 <= 1e-5) and the reference's (<= 1e-4)."""
+    d = load()
+    p, ext, wav, seis = _case(engine, d, "uneven", storage=1)
+    ref_img, ref_slf = engine.migrate_shot(p, ext, wav, seis)
+    img, slf, _ = _alone(engine, (p.replace(tile_x=tile_x), ext, wav, seis))
+    assert rel_l2(img, ref_img) <= 1e-5 and rel_l2(slf, ref_slf) <= 1e-5
+    assert rel_l2(img, d["uneven/image"]) <= 1e-4
+
+
+def test_batched_autotuner_picks_a_width(engine):
+    d = load()
+    p, ext, wav, seis = _case(engine, d, "uneven", storage=1)
+    tx, ms = engine.autotune_batched(p, members=4, steps=24)
+    assert tx in (16, 32) and ms > 0
+    # later submissions of the shape (tile_x 0) run with it and still match the plain path
+    img, slf, _ = _alone(engine, (p.replace(tile_x=0), ext, wav, seis))
+    ref_img, _ = engine.migrate_shot(p, ext, wav, seis)
+    assert rel_l2(img, ref_img) <= 1e-5
