@@ -150,8 +150,8 @@ __device__ __forceinline__ void psi_x_new(const T (&W)[9][4], T (&ps)[4], T ab, 
 // then xi and the correction term, which goes back by shuffle to the lane that owns the quad
 // and is added to v there.  qb: the band's first quad in the tile; top: the top band.
 template <typename T, int WARPS>
-__device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, const T *scf, T (&v)[RXC][4],
-                                            int x0, int z0, int qb, int nq, bool top)
+__device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, const T *scf, T (&dzo)[RXC][4],
+                                            bool (&czo)[RXC], int x0, int z0, int qb, int nq, bool top)
 {
     static_assert(RXC == 2, "one column per half-warp");
     const Geom &g = a.g;
@@ -215,7 +215,8 @@ __device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, c
         }
         st4((top ? a.xi_t : a.xi_b) + o, xz);
     }
-    // the correction terms back to the lanes owning the quads (lane = quad of the tile)
+    // the correction terms back to the lanes owning the quads (lane = quad of the tile);
+    // czo: the owner's column gets a z correction on this quad
     const int kk = lane - qb;
     const bool mine = kk >= 0 && kk < nq;
     const int src = mine ? kk : 0;
@@ -223,14 +224,10 @@ __device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, c
     const bool qCo = zo + 4 > zlo && zo < zhi;
 #pragma unroll
     for (int r = 0; r < RXC; ++r) {
-        T d[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) d[j] = __shfl_sync(0xffffffffu, dZ[j], 16 * r + src);
+        for (int j = 0; j < 4; ++j) dzo[r][j] = __shfl_sync(0xffffffffu, dZ[j], 16 * r + src);
         const int xo = x0 + warp * RXC + r;
-        if (mine && qCo && xo < g.dimx && (top || (xo >= 4 && xo < g.dimx - 4))) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) v[r][j] = v[r][j] + d[j];
-        }
+        czo[r] = mine && qCo && xo < g.dimx && (top || (xo >= 4 && xo < g.dimx - 4));
     }
 }
 
@@ -386,15 +383,28 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
         }
     }
 
-    // ---- a top or bottom tile without x-strips whose band fits a half-warp
-    if (!tX && tZ) {
+    // ---- z-strips of a tile whose band fits a half-warp (top and bottom tiles, corners
+    // included): the correction terms of the thread's own quads, applied below in strip order
+    T dZh[RXC][4];
+    bool cZh[RXC] = {false, false};
+    bool zhalf = false;
+    if (tZ) {
         const bool hasT = z0 < g.thu, hasB = zend > g.zb0;
         if (hasT != hasB) {
             const int qb = hasT ? 0 : (max(g.zb0, z0) - z0) >> 2;
             const int qe = ((hasT ? min(g.thu, zend) : zend) - z0 + 3) >> 2;
             if (qe - qb <= 16) {
-                cpml_z_half<T, WARPS>(a, su, scf, v, x0, z0, qb, qe - qb, hasT);
-                return;
+                cpml_z_half<T, WARPS>(a, su, scf, dZh, cZh, x0, z0, qb, qe - qb, hasT);
+                zhalf = true;
+                if (!tX) {
+#pragma unroll
+                    for (int r = 0; r < RXC; ++r)
+                        if (cZh[r]) {
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) v[r][j] = v[r][j] + dZh[r][j];
+                        }
+                    return;
+                }
             }
         }
     }
@@ -409,7 +419,7 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
         const int x = x0 + warp * RXC + r;
 #pragma unroll
         for (int j = 0; j < 4; ++j) { psZ[r][j] = (T)0; xZ[r][j] = (T)0; }
-        if (tZ && (inTa || inBa) && x < g.dimx) {
+        if (tZ && !zhalf && (inTa || inBa) && x < g.dimx) {
             const size_t o = inTa ? (size_t)x * g.st + zq : (size_t)x * g.sb + (zq - g.zb0);
             ld4((inTa ? a.psi_t : a.psi_b) + o, psZ[r]);
             if (qT || qB) ld4((inTa ? a.xi_t : a.xi_b) + o, xZ[r]);
@@ -420,7 +430,7 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
     // neighbours' by shuffle, the correction term; the corrections applied in strip order
     float aa[4] = {0.f, 0.f, 0.f, 0.f}, bz[4] = {0.f, 0.f, 0.f, 0.f};
     const int zlo = inTa ? 4 : g.dimz - g.thd + 4, zhi = inTa ? g.thu - 4 : g.dimz - 4;
-    if (tZ && (inTa || inBa)) {
+    if (tZ && !zhalf && (inTa || inBa)) {
         const float *pa = inTa ? a.a_t + zq : a.a_b + (zq - g.zb0);
         const float *pb = inTa ? a.b_t + zq : a.b_b + (zq - g.zb0);
         const float4 av = *reinterpret_cast<const float4 *>(pa);
@@ -434,7 +444,11 @@ __device__ __forceinline__ void cpml_fused(const StepArgs<T> &a, T *u8, T *sprv,
         const bool left = cX[r] && x < g.thl;
         T dZ[4] = {(T)0, (T)0, (T)0, (T)0};
         bool cZ = false;
-        if (tZ) {
+        if (zhalf) {
+            cZ = cZh[r];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dZ[j] = dZh[r][j];
+        } else if (tZ) {
             const bool arr = (inTa || inBa) && x < g.dimx;
             cZ = arr && (qT || (qB && x >= 4 && x < g.dimx - 4));   // the top rows cover every column
             T zz[12];
