@@ -161,8 +161,8 @@ def algorithmic_bytes(p):
                      + 4 B per ring cell read + 4 B per receiver (seismogram row)
                      + imaging every time_slices steps: 32 B per interior cell (FP64
                        image and self image read+write), averaged per launch
-    k_psi          : 12 B per psi cell (u read, psi read+write): the batched members' psi
-                     kernel (k_bpsi)."""
+    k_bpsi         : 12 B per psi cell (u read, psi read+write): the batched members' psi
+                     kernel."""
     dx, dz = p.dim_x, p.dim_z
     cells = dx * dz
     thl, thr, thu, thd = p.th_left, p.th_right, p.th_up, p.th_down
@@ -177,7 +177,7 @@ def algorithmic_bytes(p):
     fwd = 16 * cells + 16 * corr + 4 * ring
     bwd = 16 * cells + 16 * corr + 12 * region + 4 * ring + 4 * p.rec_count + 32 * interior / p.time_slices
     batched_fwd = 16 * cells + 12 * corr + 4 * ring + 12 * psi   # k_mstep + k_bpsi + k_bstrip
-    return {"k_step_fwd": fwd, "k_step_bwd": bwd, "k_psi": 12 * psi, "batched_fwd_step": batched_fwd}
+    return {"k_step_fwd": fwd, "k_step_bwd": bwd, "k_bpsi": 12 * psi, "batched_fwd_step": batched_fwd}
 
 
 def hbm_peak():

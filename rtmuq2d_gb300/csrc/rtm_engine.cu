@@ -2,7 +2,8 @@
 // the forward / adjoint time loops, and the C ABI declared in include/rtm_gpu.h.
 //
 // The time loops replace SRC/forward_modeling.c:98-130 and SRC/backward_modeling.c:268-297.
-// One step = k_psi (CPML psi update) + k_step (everything else, fused).  The forward
+// One step = one k_step launch (stencil, CPML psi and corrections, source, receivers, storage,
+// reconstruction and imaging, fused).  The forward
 // pass leaves u_nt, u_{nt-1} and the stored source wavefield (rings or snapshots) in HBM;
 // the adjoint pass consumes them in place of ./TEMPORARY_FILES.
 #include <cuda.h>

@@ -97,7 +97,8 @@ __host__ __device__ __forceinline__ int boundary_tiles(const Geom &g)
     return g.tiles_x * nzb + (g.nxl + (g.tiles_x - g.xr0)) * (g.tiles_z - nzb);
 }
 
-// Number of psi quads of each strip (k_psi's enumeration: left, top, right, bottom).
+// Number of psi quads of each strip (the batched psi kernel k_bpsi's enumeration: left, top,
+// right, bottom).
 __host__ __device__ __forceinline__ void psi_counts(const Geom &g, int (&n)[4])
 {
     const int nlr = (g.dimz - 8 + 3) / 4;

@@ -242,8 +242,11 @@ __device__ __forceinline__ void cpml_z_half(const StepArgs<T> &a, const T *su, c
 //     the u rows of the outermost halo columns, which nothing reads after that; the
 //     corrections read both;
 //   * z-strips (top, bottom): every tile row holds a whole band plus 4 rows, so a lane
-//     computes the psi of its own quad from the tile's z line and takes its neighbours' from
-//     the lanes above and below (warp shuffles).
+//     computes the psi of a quad from the tile's z line and takes its neighbours' from the
+//     lanes above and below (warp shuffles).  When the band has at most 16 quads (a CPML of
+//     up to 64 cells) it goes to half-warps, one column per thread (cpml_z_half), and the
+//     correction terms come back to the quads' owners; otherwise each lane does its own quad
+//     of both its columns.
 // u8: the stage's current-field area (tile column c at row c + 8; 4-halo tiles fill rows
 // 4 .. TXC + 12); sprv: the stage's u_prev tile.  The previous psi, xi and the profiles come
 // from global memory, each thread's loads issued before the work that needs them.
