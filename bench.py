@@ -366,6 +366,30 @@ def summary(line):
     return out
 
 
+def _round_floats(v, sig=5):
+    if isinstance(v, float):
+        return float("%.*g" % (sig, v))
+    if isinstance(v, dict):
+        return {k: _round_floats(x, sig) for k, x in v.items()}
+    if isinstance(v, list):
+        return [_round_floats(x, sig) for x in v]
+    return v
+
+
+def compact_line(line):
+    """The bench line as printed: the contract's keys, then the summary of every form (early,
+    so that a reader keeping only the head of the line still sees batched, served and parity),
+    then the details, floats to 5 significant digits."""
+    line = dict(line)
+    line["summary"] = summary(line)
+    head = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+            "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "gpu_launches", "roofline",
+            "cpu_baseline", "clocks", "summary")
+    out = {k: line[k] for k in head if k in line}
+    out.update({k: v for k, v in line.items() if k not in out})
+    return _round_floats(out)
+
+
 def run_batched(args, eng, rank=0, ws=1):
     """The batched UQ ensemble through the serving engine: every member resident at once,
     advanced together by the batched step kernels.  Timed from the first submit (host
@@ -954,8 +978,7 @@ def run_gpu(args):
             "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
             "clocks": sampler.summary(), "precision": precision, "batched": batched, "served": served,
             "parity": parity}
-    line["summary"] = summary(line)
-    print(json.dumps(line), flush=True)
+    print(json.dumps(compact_line(line)), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
