@@ -116,14 +116,15 @@ __device__ __forceinline__ void margs(const BMember<T> &M, int t, int role, MArg
 // For one quad of a strip: xi_n = b xi_{n-1} + a (D2(u_n) / dx^2 + D1(psi_n) / dx) and the
 // correction coef dx^2 (D1(psi_n)/dx + xi_n) that the reference adds to u_{n+1}
 // (absorbingBoundaryCondition.c:191-217 left, 237-263 top, 283-310 right, 330-357 bottom);
-// same arithmetic as cpml_x_quad / cpml_z_quad (rtm_step.cuh).  c4 gets the correction.
+// the same arithmetic, in the same operand order, as the single-migration step kernel's CPML
+// pass (cpml_fused / cpml_z_half, rtm_step.cuh).  c4 gets the correction.
 template <typename T>
 __device__ __forceinline__ void strip_x_quad(const T *psi, T *xi, const T *ucol, size_t P, T ab, T bb,
                                              const T (&cf)[4], int zq, int zlo, int zhi, T h1, T h2, T h3,
                                              bool fresh, T (&c4)[4])
 {
     // dpsi (B coefficients) and D2 along x (AC coefficients) accumulated one row pair at a
-    // time, +-4 first, in the operand order of cpml_x_quad / d2x_w, so that only two rows of
+    // time, +-4 first, in the operand order of d1x_w / d2x_w (rtm_step.cuh), so that only two rows of
     // each field are live at once
     T acc[4], d2[4];
     {
