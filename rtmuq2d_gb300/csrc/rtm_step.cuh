@@ -594,38 +594,56 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, T *stage, int t,
                           (image_t && !image_fast) || (flags & F_NO_STENCIL);
 
     // ================= the propagated field: leapfrog =================
+    // Two copies of the column loop, chosen once per tile, so that the plain interior tiles
+    // carry none of the boundary tiles' per-cell range tests (the compiler would otherwise
+    // predicate them into every tile).
     T v[RXC][4];
     {
         T W[9][4];
 #pragma unroll
         for (int m = 0; m < 8; ++m) ld4(su + (row0 + m) * SZ + zi, W[m]);
+        if (!boundary) {
 #pragma unroll
-        for (int r = 0; r < RXC; ++r) {
-            ld4(su + (row0 + r + 8) * SZ + zi, W[8]);
-            T zz[12];
-            z_line<T>(su, row0 + r + 4, zi, W[4], zz);
-            T prv[4], cf[4];
-            ld4(sprv + (row0 + r) * TZ + 4 * lane, prv);
-            ld4(scf + (row0 + r) * TZ + 4 * lane, cf);
-            const int x = xb + r;
+            for (int r = 0; r < RXC; ++r) {
+                ld4(su + (row0 + r + 8) * SZ + zi, W[8]);
+                T zz[12];
+                z_line<T>(su, row0 + r + 4, zi, W[4], zz);
+                T prv[4], cf[4];
+                ld4(sprv + (row0 + r) * TZ + 4 * lane, prv);
+                ld4(scf + (row0 + r) * TZ + 4 * lane, cf);
+                const int x = xb + r;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const T s = cf[j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - prv[j];
-                if (!boundary) v[r][j] = s;
-                else {
-                    const int z = zq + j;
-                    v[r][j] = (!(flags & F_NO_STENCIL) && x >= 4 && x < g.dimx - 4 && z >= 4 &&
-                               z < g.dimz - 4) ? s : prv[j];
-                }
-            }
-            if (!boundary) {
+                for (int j = 0; j < 4; ++j) v[r][j] = cf[j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - prv[j];
                 if (zok && x < g.dimx) st4(a.u_next + (size_t)x * P + zq, v[r]);
                 if (snap_fast) st4(reinterpret_cast<T *>(a.store) + (size_t)(x - g.thl) * P + zq, v[r]);
+#pragma unroll
+                for (int m = 0; m < 8; ++m)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
             }
+        } else {
+            const bool stencil = !(flags & F_NO_STENCIL);
 #pragma unroll
-            for (int m = 0; m < 8; ++m)
+            for (int r = 0; r < RXC; ++r) {
+                ld4(su + (row0 + r + 8) * SZ + zi, W[8]);
+                T zz[12];
+                z_line<T>(su, row0 + r + 4, zi, W[4], zz);
+                T prv[4], cf[4];
+                ld4(sprv + (row0 + r) * TZ + 4 * lane, prv);
+                ld4(scf + (row0 + r) * TZ + 4 * lane, cf);
+                const int x = xb + r;
+                const bool xs = stencil && x >= 4 && x < g.dimx - 4;
 #pragma unroll
-                for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
+                for (int j = 0; j < 4; ++j) {
+                    const T sv = cf[j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - prv[j];
+                    const int z = zq + j;
+                    v[r][j] = (xs && z >= 4 && z < g.dimz - 4) ? sv : prv[j];
+                }
+#pragma unroll
+                for (int m = 0; m < 8; ++m)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
+            }
         }
     }
 
