@@ -743,6 +743,37 @@ __device__ __forceinline__ void step_tile(const StepArgs<T> &a, T *stage, int t,
 #pragma unroll
         for (int m = 0; m < 8; ++m) ld4(ss + (row0 + m) * SZ + zi, W[m]);
     }
+    // Plain reconstruction tiles (inside the region, no source cell, imaged without per-cell
+    // tests if at all): their own copy of the column loop, free of the per-cell range tests
+    // of the general one below.
+    if (recon && in_region && !src_t && (!image_t || image_fast)) {
+#pragma unroll
+        for (int r = 0; r < RXC; ++r) {
+            const int x = xb + r;
+            ld4(ss + (row0 + r + 8) * SZ + zi, W[8]);
+            T zz[12];
+            z_line<T>(ss, row0 + r + 4, zi, W[4], zz);
+            T sp[4], cf[4], s[4];
+            ld4(ssp + (row0 + r) * TZ + 4 * lane, sp);
+            ld4(scf + (row0 + r) * TZ + 4 * lane, cf);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) s[j] = cf[j] * lap8<T>(W, zz, j) + (T)2.0f * W[4][j] - sp[j];
+            if (zok) {
+                st4(a.s_next + (size_t)x * P + zq, s);
+                if (image_t) {
+                    T rv[4];
+                    ld4(a.u_next + (size_t)x * P + zq, rv);
+                    const size_t o = (size_t)(x - g.thl) * P + zq;
+                    image_quad<T>(a.img + o, a.slf + o, s, rv);
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 8; ++m)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) W[m][j] = W[m + 1][j];
+        }
+        return;
+    }
 #pragma unroll
     for (int r = 0; r < RXC; ++r) {
         const int x = xb + r;
